@@ -1,0 +1,343 @@
+"""Benchmark: geodesic Mrays/s on the 1920x1080, 120-frame fly-through.
+
+A step is one pass of the tracer over the whole fly-through (120 frames of
+1920x1080 = 248.8 M rays), replayed as one captured CUDA graph. Lines:
+
+- ``value``: the mixed-precision batched tracer (persistent work-stealing
+  launch over all 120 frames, FP32 bulk, FP64 for rays within the band of
+  the critical impact parameter and for disc-crossing refinement),
+  device-resident inputs, L2 flushed between timed steps.
+- ``variants.plain_fp32``: the plain FP32 tracer (one thread per pixel).
+- ``e2e``: the same mixed tracer through the C ABI's bh_render with host
+  buffers: scene upload, render and the BGR8 (CV_8UC3) frames copied back to
+  pinned host memory inside the timed region.
+- ``cpu_baseline``: the reference's own render loop (oracle/_ref, its
+  20+20-step trapezoid scheme, FP64) on the host cores, on a bounded sample of
+  the same fly-through.
+
+``--impl reference`` times only that reference CPU render (rank 0).
+Multi-GPU: every rank renders its own copy of the fly-through (replicas, no
+collective on the data path); value = all ranks' rays / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES, WIDTH, HEIGHT = 120, 1920, 1080
+METRIC = "geodesic Mrays/s 1080p, plain vs mixed-prec batched @<=1e-4 rad; adjoint Mrays/s"
+WORKLOAD = "fly-through 120 frames 1920x1080, r 30M->8M spiral, incl 60->89 deg, FoV 60 deg, RK4 dphi=0.01, " \
+           "<=4000 steps, escape 100M"
+CPU_SAMPLE_FRAMES = list(range(0, FRAMES, 15))  # 8 frames
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference(scenes, frames_idx, threads: int):
+    """The reference's own render loop on the host cores; falls back to the
+    oracle's restatement of it. Returns (Mrays/s, threads, kind, sample)."""
+    from oracle import oracle, refbridge
+    sample = [scenes[i] for i in frames_idx]
+    desc = f"{len(sample)} of {len(scenes)} fly-through frames ({frames_idx[0]}..{frames_idx[-1]} step " \
+           f"{frames_idx[1] - frames_idx[0] if len(frames_idx) > 1 else 0}) at {WIDTH}x{HEIGHT}, full frames"
+    try:
+        if not refbridge.available():
+            raise RuntimeError("reference runner unavailable")
+        # the reference renders its own scene type: planar disc mapping is its
+        # only mapping; the geometry and ray count are the workload's
+        _, timing = refbridge.render(sample, threads=threads, timed=True)
+        return timing["mrays_per_s"], timing["threads"], "reference", desc
+    except Exception as exc:  # fall back to the restatement
+        print(f"# reference runner not used: {exc}", file=sys.stderr)
+        t0 = time.perf_counter()
+        for sc in sample:
+            oracle.render_ref(sc, threads=threads)
+        dt = time.perf_counter() - t0
+        rays = len(sample) * WIDTH * HEIGHT
+        return rays / dt / 1e6, threads or oracle.max_threads(), "port", desc
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from blackhole_8_gb300 import scene as S
+    scenes = S.flythrough(FRAMES, WIDTH, HEIGHT)
+    threads = os.cpu_count() or 1
+    sample = [0, 40, 80, 119]
+    for _ in range(args.warmup):
+        cpu_reference(scenes, sample, threads)
+    vals = []
+    kind = desc = None
+    used = threads
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, used, kind, desc = cpu_reference(scenes, sample, threads)
+        vals.append(v)
+    wall = time.perf_counter() - t_all
+    value = sum(vals) / len(vals)
+    rays_step = len(sample) * WIDTH * HEIGHT
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(rays_step / (value * 1e6) * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_per_step": desc, "integrator": "reference trapezoid 20+20"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": used, "kind": kind,
+                         "sample": desc},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": round(wall, 2),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    from blackhole_8_gb300 import build
+    build.build()
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+    from blackhole_8_gb300.render import Renderer
+
+    scenes = S.flythrough(FRAMES, WIDTH, HEIGHT)
+    r = Renderer(local)
+    cs = r.c_scenes(scenes)
+    stream = torch.cuda.ExternalStream(r.stream)
+    px = torch.empty((FRAMES, HEIGHT, WIDTH, 4), dtype=torch.uint8, device="cuda")
+    frames = (capi.Frame * FRAMES)()
+    for i in range(FRAMES):
+        frames[i].pixels = px[i].data_ptr()
+        frames[i].hit_class = None
+        frames[i].aux = None
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def time_sequence(opts, launches_per_step):
+        seq = r.sequence(cs, frames, opts)
+        for _ in range(args.warmup):
+            seq.launch()
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for a, b in evs:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a.record(stream)
+            seq.launch()
+            b.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+        ms = [a.elapsed_time(b) for a, b in evs]
+        st = seq.stats()
+        seq.close()
+        return sum(ms) / len(ms), st, wall, launches_per_step * args.steps
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    fp32_tflops, sm_count = r.fp32_peak()
+    fp64_tflops = r.fp64_peak()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    mixed_opts = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
+    plain_opts = capi.default_options(precision=capi.PRECISION_FP32, schedule=capi.SCHEDULE_GRID)
+    ms_mixed, st_mixed, wall_mixed, launches_mixed = time_sequence(mixed_opts, 2)
+    ms_plain, st_plain, wall_plain, launches_plain = time_sequence(plain_opts, 1)
+    clock_info = clocks.stop()
+
+    rays_step = FRAMES * WIDTH * HEIGHT
+    ms_mixed_max = max_over_ranks(ms_mixed)
+    ms_plain_max = max_over_ranks(ms_plain)
+    value = rays_step * world / (ms_mixed_max * 1e-3) / 1e6
+    plain_value = rays_step * world / (ms_plain_max * 1e-3) / 1e6
+
+    # roofline: algorithmic FP32 flops of the RK4 steps of the dominant (FP32)
+    # pass per launch over the launch's device time
+    fp32_steps = st_mixed.steps - st_mixed.band_steps
+    achieved = fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms_mixed * 1e-3) / 1e12
+    plain_achieved = st_plain.steps * capi.RK4_FLOPS_PER_STEP / (ms_plain * 1e-3) / 1e12
+
+    # end to end through bh_render with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((FRAMES, HEIGHT, WIDTH, 3), dtype=torch.uint8, pin_memory=True)
+        hframes = (capi.Frame * FRAMES)()
+        for i in range(FRAMES):
+            hframes[i].pixels = host[i].data_ptr()
+            hframes[i].hit_class = None
+            hframes[i].aux = None
+        e2e_opts = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
+                                        format=capi.FORMAT_BGR8)
+        for _ in range(max(1, args.warmup)):
+            r.render_into(cs, hframes, e2e_opts)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r.render_into(cs, hframes, e2e_opts)
+        dt = (time.perf_counter() - t0) / args.steps
+        dt = max_over_ranks(dt)
+        st_e2e = r.stats()
+        e2e = {"value": round(rays_step * world / dt / 1e6, 3), "unit": "Mrays/s",
+               "h2d_bytes_per_step": int(st_e2e.h2d_bytes),
+               "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
+               "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, used, kind, desc = cpu_reference(scenes, CPU_SAMPLE_FRAMES, os.cpu_count() or 1)
+        cpu = {"value": round(v, 4), "unit": "Mrays/s", "cores": used, "kind": kind, "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_mixed_max, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "tracer": "mixed-precision batched (persistent, FP64 band "
+                                                       f"|b-b_c|<{mixed_opts.band} M)",
+                       "frames": FRAMES, "width": WIDTH, "height": HEIGHT,
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+            "variants": {
+                "mixed_batched": {"mrays_per_s": round(value, 3), "ms_per_step": round(ms_mixed_max, 3),
+                                  "steps_total": int(st_mixed.steps), "band_rays": int(st_mixed.band_rays),
+                                  "band_fraction": st_mixed.band_rays / rays_step,
+                                  "band_steps": int(st_mixed.band_steps), "band_overflow": int(st_mixed.band_overflow),
+                                  "wall_s": round(wall_mixed, 3)},
+                "plain_fp32": {"mrays_per_s": round(plain_value, 3), "ms_per_step": round(ms_plain_max, 3),
+                               "steps_total": int(st_plain.steps),
+                               "fp32_tflops": round(plain_achieved, 3),
+                               "frac_of_fp32_peak": round(plain_achieved / fp32_tflops, 4),
+                               "wall_s": round(wall_plain, 3)},
+            },
+            "roofline": {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_tflops, 3),
+                         "unit": "TFLOP/s", "frac": round(achieved / fp32_tflops, 4), "traffic": None,
+                         "peak_source": "measured in this run: FMA microbenchmark bh_probe_fp32_peak",
+                         "flops_per_step": capi.RK4_FLOPS_PER_STEP, "sm_count": sm_count,
+                         "fp64_peak_tflops_measured": round(fp64_tflops, 3)},
+            "clocks": clock_info,
+            "e2e": e2e,
+            "gpu_launches": launches_mixed + launches_plain,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    r.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

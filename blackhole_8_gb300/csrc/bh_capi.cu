@@ -1,0 +1,842 @@
+// C ABI of the GB300 geodesic ray tracer (declared in include/bh_gb300.h).
+//
+// Host side of the drop-in for the reference's frame body
+// (blackhole_solution_test.cc:161-298): validates POD scenes, resolves them
+// into DevScene records (positions relative to the hole, FP64 + FP32 copies),
+// stages them through pinned memory, launches the kernels on the context's
+// stream and, for bh_render, copies the frames back.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bh_internal.h"
+
+using bhgb::DevCounters;
+using bhgb::DevScene;
+using bhgb::DevTexture;
+using bhgb::LaunchParams;
+
+namespace {
+
+struct TexEntry {
+  uchar4* texels = nullptr;
+  int32_t width = 0, height = 0;
+  bool alive = false;
+};
+
+template <typename T>
+struct PinnedBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;
+};
+
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;
+};
+
+}  // namespace
+
+struct bh_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<TexEntry> textures;
+  PinnedBuf<DevScene> h_scenes;
+  DevBuf<DevScene> d_scenes;
+  DevCounters* d_counters = nullptr;
+  DevCounters* h_counters = nullptr;
+  DevBuf<uint32_t> band_list;
+  DevBuf<uint8_t> out_arena;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_staged = nullptr;
+  bool staged_pending = false;
+  bool stats_valid = false;
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  bh_render_stats last{};
+};
+
+struct bh_sequence {
+  bh_ctx* ctx = nullptr;
+  int32_t n = 0;
+  bh_render_options opts{};
+  std::vector<bh_scene> scenes;
+  std::vector<bh_frame> frames;
+  DevScene* h_scenes = nullptr;   // pinned, owned
+  DevScene* d_scenes = nullptr;   // owned
+  DevCounters* d_counters = nullptr;
+  uint32_t* band_list = nullptr;
+  uint32_t band_capacity = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev_done = nullptr;
+  bool launched = false;
+};
+
+namespace {
+
+int set_err(bh_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+int cuda_err(bh_ctx* ctx, cudaError_t e, const char* what) {
+  int code = BH_ERR_CUDA;
+  if (e == cudaErrorMemoryAllocation) code = BH_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorIllegalAddress || e == cudaErrorLaunchFailure || e == cudaErrorIllegalInstruction ||
+      e == cudaErrorMisalignedAddress || e == cudaErrorHardwareStackError)
+    code = BH_ERR_DEVICE_FAULT;
+  return set_err(ctx, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define BH_CUDA(ctx, call)                                   \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call);  \
+  } while (0)
+
+template <typename T>
+int ensure_dev(bh_ctx* ctx, DevBuf<T>& b, size_t n) {
+  if (b.cap >= n) return BH_OK;
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.cap = 0;
+  BH_CUDA(ctx, cudaMalloc(&b.ptr, n * sizeof(T)));
+  b.cap = n;
+  return BH_OK;
+}
+
+template <typename T>
+int ensure_pinned(bh_ctx* ctx, PinnedBuf<T>& b, size_t n) {
+  if (b.cap >= n) return BH_OK;
+  if (b.ptr) cudaFreeHost(b.ptr);
+  b.ptr = nullptr;
+  b.cap = 0;
+  BH_CUDA(ctx, cudaMallocHost(&b.ptr, n * sizeof(T)));
+  b.cap = n;
+  return BH_OK;
+}
+
+bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+int bytes_per_pixel(int32_t format) { return format == BH_FORMAT_BGR8 ? 3 : 4; }
+
+void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
+  bh_default_options(out);
+  if (!in) return;
+  *out = *in;
+  bh_render_options d;
+  bh_default_options(&d);
+  if (out->max_steps == 0) out->max_steps = d.max_steps;
+  if (out->step == 0) out->step = d.step;
+  if (out->r_escape == 0) out->r_escape = d.r_escape;
+  if (out->band < 0) out->band = d.band;
+  if (out->block_x == 0) out->block_x = d.block_x;
+  if (out->block_y == 0) out->block_y = d.block_y;
+  if (out->threads_per_block == 0) out->threads_per_block = d.threads_per_block;
+  if (out->refill_threshold == 0) out->refill_threshold = d.refill_threshold;
+}
+
+int validate_options(bh_ctx* ctx, const bh_render_options& o) {
+  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
+  if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
+  if (o.integrator == BH_INTEGRATOR_REF_TRAPEZOID && o.precision == BH_PRECISION_MIXED)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "MIXED precision applies to the RK4 integrator only");
+  if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown raygen %d", o.raygen);
+  if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown format %d", o.format);
+  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown schedule %d", o.schedule);
+  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.integrator != BH_INTEGRATOR_RK4)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "the persistent schedule runs the RK4 integrator only");
+  if (!(o.step > 0 && o.step <= 1.0)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "step must be in (0, 1]");
+  if (o.max_steps < 1 || o.max_steps > 100000000)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e8]");
+  if (!(o.r_escape > 2.0) || !std::isfinite(o.r_escape))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "r_escape must exceed the horizon (2 M)");
+  if (!(o.band >= 0) || !std::isfinite(o.band)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band must be >= 0");
+  if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 1024 || (o.block_x * o.block_y) % 32 != 0)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 1024");
+  if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "threads_per_block must be a multiple of 32 in [32, 256]");
+  if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
+  if (o.refill_threshold < 1 || o.refill_threshold > 32)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");
+  return BH_OK;
+}
+
+int texture_ok(bh_ctx* ctx, int32_t id) {
+  return id >= 0 && id < (int32_t)ctx->textures.size() && ctx->textures[id].alive;
+}
+
+int validate_scene(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_options& o) {
+  const bh_camera& c = s.camera;
+  if (c.width < 1 || c.height < 1 || c.width > 32768 || c.height > 32768)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: image size %dx%d out of range", i, c.width, c.height);
+  if (!finite3(c.position) || !finite3(c.axis_x) || !finite3(c.axis_y) || !finite3(c.axis_z) ||
+      !std::isfinite(c.focus_len))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: camera has a non-finite value", i);
+  if (!finite3(s.hole.position) || !(s.hole.mass > 0) || !std::isfinite(s.hole.mass))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: hole mass must be positive and finite", i);
+  if (s.background != -1 && !texture_ok(ctx, s.background))
+    return set_err(ctx, BH_ERR_BAD_TEXTURE, "scene %d: background texture %d is not valid", i, s.background);
+  const double rel[3] = {c.position[0] - s.hole.position[0], c.position[1] - s.hole.position[1],
+                         c.position[2] - s.hole.position[2]};
+  if (o.integrator == BH_INTEGRATOR_RK4 && std::sqrt(dot3(rel, rel)) >= o.r_escape * s.hole.mass)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: camera lies outside the escape radius", i);
+  if (s.disc.enabled) {
+    const bh_disc& d = s.disc;
+    if (!texture_ok(ctx, d.texture))
+      return set_err(ctx, BH_ERR_BAD_TEXTURE, "scene %d: disc texture %d is not valid", i, d.texture);
+    if (!finite3(d.center) || !finite3(d.normal) || !finite3(d.corner) || !finite3(d.edge_s1) ||
+        !finite3(d.edge_s2) || !std::isfinite(d.r_inner) || !std::isfinite(d.r_outer))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: disc has a non-finite value", i);
+    if (!(d.r_inner >= 0) || !(d.r_outer > d.r_inner))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: disc needs 0 <= r_inner < r_outer", i);
+    if (d.mapping != BH_DISC_MAP_REF_PLANAR && d.mapping != BH_DISC_MAP_POLAR)
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: unknown disc mapping %d", i, d.mapping);
+    const double nn = dot3(d.normal, d.normal);
+    if (!(std::fabs(nn - 1.0) < 1e-6))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: disc normal must be a unit vector", i);
+    if (!(dot3(d.edge_s1, d.edge_s1) > 0) || !(dot3(d.edge_s2, d.edge_s2) > 0))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: disc quad edges must be non-zero", i);
+    if (o.integrator == BH_INTEGRATOR_RK4) {
+      const double off[3] = {d.center[0] - s.hole.position[0], d.center[1] - s.hole.position[1],
+                             d.center[2] - s.hole.position[2]};
+      const double scale = std::max(1.0, std::sqrt(dot3(off, off)) + s.hole.mass);
+      if (std::fabs(dot3(d.normal, off)) > 1e-9 * scale)
+        return set_err(ctx, BH_ERR_UNSUPPORTED,
+                       "scene %d: the RK4 integrator needs the disc plane to contain the hole", i);
+      if (d.r_outer >= o.r_escape * s.hole.mass)
+        return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: disc extends past the escape radius", i);
+    }
+  }
+  return BH_OK;
+}
+
+void set3(double* dst, float* dstf, double a, double b, double c) {
+  dst[0] = a; dst[1] = b; dst[2] = c;
+  dstf[0] = float(a); dstf[1] = float(b); dstf[2] = float(c);
+}
+
+void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_render_options& o,
+                   int64_t ray_begin, DevScene* d) {
+  std::memset(d, 0, sizeof(*d));
+  const bh_camera& c = s.camera;
+  const double* h = s.hole.position;
+  const double fv[3] = {c.axis_x[0] * c.focus_len, c.axis_x[1] * c.focus_len, c.axis_x[2] * c.focus_len};
+  set3(d->F, d->F_f, c.position[0] - h[0], c.position[1] - h[1], c.position[2] - h[2]);
+  if (o.raygen == BH_RAYGEN_REF)
+    set3(d->E0, d->E0_f, c.position[0] - fv[0], c.position[1] - fv[1], c.position[2] - fv[2]);
+  else
+    set3(d->E0, d->E0_f, -fv[0], -fv[1], -fv[2]);
+  set3(d->vy, d->vy_f, c.axis_y[0], c.axis_y[1], c.axis_y[2]);
+  set3(d->vz, d->vz_f, c.axis_z[0], c.axis_z[1], c.axis_z[2]);
+  const double M = s.hole.mass;
+  d->mass = M;
+  d->b_c = 3.0 * std::sqrt(3.0) * M;  // blackhole_solution.h:25
+  d->r_h = 2.0 * M;                    // blackhole_solution.h:57
+  d->half_w = c.width / 2.0;
+  d->half_h = c.height / 2.0;
+  d->width = c.width;
+  d->height = c.height;
+  d->tiles_x = (c.width + 7) / 8;
+  d->ray_begin = ray_begin;
+  d->disc_on = s.disc.enabled ? 1 : 0;
+  if (s.disc.enabled) {
+    const bh_disc& q = s.disc;
+    set3(d->dc, d->dc_f, q.center[0] - h[0], q.center[1] - h[1], q.center[2] - h[2]);
+    set3(d->dn, d->dn_f, q.normal[0], q.normal[1], q.normal[2]);
+    set3(d->dv1, d->dv1_f, q.corner[0] - h[0], q.corner[1] - h[1], q.corner[2] - h[2]);
+    set3(d->ds1, d->ds1_f, q.edge_s1[0], q.edge_s1[1], q.edge_s1[2]);
+    set3(d->ds2, d->ds2_f, q.edge_s2[0], q.edge_s2[1], q.edge_s2[2]);
+    d->s1_len = std::sqrt(dot3(q.edge_s1, q.edge_s1));
+    d->s2_len = std::sqrt(dot3(q.edge_s2, q.edge_s2));
+    const double e1[3] = {q.edge_s1[0] / d->s1_len, q.edge_s1[1] / d->s1_len, q.edge_s1[2] / d->s1_len};
+    double e2[3] = {q.normal[1] * e1[2] - q.normal[2] * e1[1], q.normal[2] * e1[0] - q.normal[0] * e1[2],
+                    q.normal[0] * e1[1] - q.normal[1] * e1[0]};
+    const double l2 = std::sqrt(dot3(e2, e2));
+    if (l2 > 0) { e2[0] /= l2; e2[1] /= l2; e2[2] /= l2; }
+    set3(d->de1, d->de1_f, e1[0], e1[1], e1[2]);
+    set3(d->de2, d->de2_f, e2[0], e2[1], e2[2]);
+    d->r_in = q.r_inner;
+    d->r_out = q.r_outer;
+    d->disc_map = q.mapping;
+    const TexEntry& t = ctx->textures[q.texture];
+    d->disc_tex = DevTexture{t.texels, t.width, t.height};
+  }
+  d->has_bg = s.background >= 0 ? 1 : 0;
+  if (s.background >= 0) {
+    const TexEntry& t = ctx->textures[s.background];
+    d->bg_tex = DevTexture{t.texels, t.width, t.height};
+  }
+  d->mass_f = float(d->mass);
+  d->b_c_f = float(d->b_c);
+  d->r_h_f = float(d->r_h);
+  d->r_in_f = float(d->r_in);
+  d->r_out_f = float(d->r_out);
+  d->s1_len_f = float(d->s1_len);
+  d->s2_len_f = float(d->s2_len);
+  d->half_w_f = float(d->half_w);
+  d->half_h_f = float(d->half_h);
+  d->pixels = static_cast<uint8_t*>(f.pixels);
+  d->cls = f.hit_class;
+  d->aux = f.aux;
+}
+
+int64_t padded_rays(const bh_camera& c) {
+  return int64_t((c.width + 7) / 8) * int64_t((c.height + 3) / 4) * 32;
+}
+
+int check_inputs(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                 const bh_render_options* opts_in, bh_render_options* o) {
+  if (!ctx) return BH_ERR_INVALID_ARGUMENT;
+  if (!scenes || !frames || n < 1 || n > 65535)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "need 1..65535 scenes with frames");
+  resolve_defaults(opts_in, o);
+  int rc = validate_options(ctx, *o);
+  if (rc) return rc;
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    rc = validate_scene(ctx, scenes[i], i, *o);
+    if (rc) return rc;
+    if (!frames[i].pixels) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "frame %d has no pixel buffer", i);
+    if (frames[i].aux && o->integrator != BH_INTEGRATOR_RK4)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "frame %d: aux output needs the RK4 integrator", i);
+    total += padded_rays(scenes[i].camera);
+  }
+  if (total >= (int64_t(1) << 32)) return set_err(ctx, BH_ERR_UNSUPPORTED, "too many rays in one call");
+  return BH_OK;
+}
+
+// Waits until the pinned staging buffer may be rewritten.
+int wait_staging(bh_ctx* ctx) {
+  if (ctx->staged_pending) {
+    BH_CUDA(ctx, cudaEventSynchronize(ctx->ev_staged));
+    ctx->staged_pending = false;
+  }
+  return BH_OK;
+}
+
+LaunchParams base_params(const bh_render_options& o) {
+  LaunchParams p{};
+  p.integrator = o.integrator;
+  p.precision = o.precision;
+  p.format = o.format;
+  p.raygen = o.raygen;
+  p.max_steps = o.max_steps;
+  p.step = o.step;
+  p.u_escape = 1.0 / o.r_escape;
+  p.band = o.band;
+  p.refill_threshold = o.refill_threshold;
+  return p;
+}
+
+uint32_t band_capacity_for(int64_t total) {
+  const int64_t cap = std::max<int64_t>(int64_t(1) << 20, total / 16);
+  return uint32_t(std::min<int64_t>(cap, total + 32));
+}
+
+int persistent_blocks(bh_ctx* ctx, const LaunchParams& p, const bh_render_options& o, int* blocks) {
+  int per_sm = o.blocks_per_sm;
+  if (per_sm == 0) {
+    BH_CUDA(ctx, bhgb::persistent_occupancy(p, o.threads_per_block, &per_sm));
+    if (per_sm < 1) per_sm = 1;
+  }
+  *blocks = per_sm * ctx->sm_count;
+  return BH_OK;
+}
+
+// Enqueues the kernels of one render (scenes already on the device).
+int enqueue_kernels(bh_ctx* ctx, LaunchParams& p, const bh_render_options& o, const bh_scene* scenes,
+                    int32_t n, cudaStream_t st) {
+  if (o.schedule == BH_SCHEDULE_GRID) {
+    std::vector<int32_t> w(n), h(n);
+    for (int i = 0; i < n; ++i) {
+      w[i] = scenes[i].camera.width;
+      h[i] = scenes[i].camera.height;
+    }
+    BH_CUDA(ctx, bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, st));
+  } else {
+    int blocks = 0;
+    int rc = persistent_blocks(ctx, p, o, &blocks);
+    if (rc) return rc;
+    BH_CUDA(ctx, bhgb::launch_persistent(p, o.threads_per_block, blocks, st));
+  }
+  return BH_OK;
+}
+
+// Stages the scenes, launches, and leaves the counters copy enqueued.
+int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* dframes,
+                     const bh_render_options& o, cudaStream_t st) {
+  int rc = wait_staging(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_pinned(ctx, ctx->h_scenes, n))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->d_scenes, n))) return rc;
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    resolve_scene(ctx, scenes[i], dframes[i], o, total, ctx->h_scenes.ptr + i);
+    total += padded_rays(scenes[i].camera);
+  }
+  LaunchParams p = base_params(o);
+  p.scenes = ctx->d_scenes.ptr;
+  p.n_scenes = n;
+  p.total_rays = total;
+  p.counters = ctx->d_counters;
+  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
+    const uint32_t cap = band_capacity_for(total);
+    if ((rc = ensure_dev(ctx, ctx->band_list, cap))) return rc;
+    p.band_list = ctx->band_list.ptr;
+    p.band_capacity = cap;
+  }
+  BH_CUDA(ctx, cudaMemcpyAsync(ctx->d_scenes.ptr, ctx->h_scenes.ptr, sizeof(DevScene) * n,
+                               cudaMemcpyHostToDevice, st));
+  ctx->h2d_bytes = sizeof(DevScene) * size_t(n);
+  ctx->d2h_bytes = 0;
+  BH_CUDA(ctx, cudaEventRecord(ctx->ev_staged, st));
+  ctx->staged_pending = true;
+  BH_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(DevCounters), st));
+  BH_CUDA(ctx, cudaEventRecord(ctx->ev_start, st));
+  if ((rc = enqueue_kernels(ctx, p, o, scenes, n, st))) return rc;
+  BH_CUDA(ctx, cudaEventRecord(ctx->ev_stop, st));
+  BH_CUDA(ctx, cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+  ctx->stats_valid = true;
+  return BH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bh_abi_version(void) { return BH_ABI_VERSION; }
+
+void bh_default_options(bh_render_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->integrator = BH_INTEGRATOR_RK4;
+  o->precision = BH_PRECISION_FP32;
+  o->raygen = BH_RAYGEN_REF;
+  o->format = BH_FORMAT_BGRA8;
+  o->schedule = BH_SCHEDULE_GRID;
+  o->max_steps = 4000;
+  o->step = 0.01;
+  o->r_escape = 100.0;
+  o->band = 0.01;
+  o->block_x = 32;
+  o->block_y = 4;
+  o->threads_per_block = 256;
+  o->blocks_per_sm = 0;
+  o->refill_threshold = 8;
+}
+
+int bh_create(bh_ctx** out, int device) {
+  if (!out) return BH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return BH_ERR_NO_DEVICE;
+  if (device < 0 || device >= count) return BH_ERR_INVALID_ARGUMENT;
+  bh_ctx* ctx = new (std::nothrow) bh_ctx();
+  if (!ctx) return BH_ERR_OUT_OF_MEMORY;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_stop);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counters, sizeof(DevCounters));
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, sizeof(DevCounters));
+  if (e != cudaSuccess) {
+    bh_destroy(ctx);
+    return e == cudaErrorMemoryAllocation ? BH_ERR_OUT_OF_MEMORY : BH_ERR_CUDA;
+  }
+  *out = ctx;
+  return BH_OK;
+}
+
+void bh_destroy(bh_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto& t : ctx->textures)
+    if (t.texels) cudaFree(t.texels);
+  if (ctx->h_scenes.ptr) cudaFreeHost(ctx->h_scenes.ptr);
+  if (ctx->d_scenes.ptr) cudaFree(ctx->d_scenes.ptr);
+  if (ctx->band_list.ptr) cudaFree(ctx->band_list.ptr);
+  if (ctx->out_arena.ptr) cudaFree(ctx->out_arena.ptr);
+  if (ctx->d_counters) cudaFree(ctx->d_counters);
+  if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+  if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+  if (ctx->ev_staged) cudaEventDestroy(ctx->ev_staged);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* bh_last_error(const bh_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* bh_stream(bh_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int bh_texture_create(bh_ctx* ctx, const uint8_t* texels, int32_t width, int32_t height, int32_t layout,
+                      int64_t row_stride, int32_t* out_id) {
+  if (!ctx || !out_id) return BH_ERR_INVALID_ARGUMENT;
+  if (!texels || width <= 0 || height <= 0)
+    return set_err(ctx, BH_ERR_EMPTY_TEXTURE, "empty texture (the reference terminates here)");
+  if ((int64_t)width * height > (int64_t(1) << 28))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "texture larger than 2^28 texels");
+  int cpp = 0;
+  switch (layout) {
+    case BH_TEXEL_BGR8: case BH_TEXEL_RGB8: cpp = 3; break;
+    case BH_TEXEL_BGRA8: case BH_TEXEL_RGBA8: cpp = 4; break;
+    default: return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown texel layout %d", layout);
+  }
+  if (row_stride == 0) row_stride = int64_t(width) * cpp;
+  if (row_stride < int64_t(width) * cpp) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "row stride too small");
+  std::vector<uchar4> host(size_t(width) * height);
+  for (int32_t y = 0; y < height; ++y) {
+    const uint8_t* row = texels + y * row_stride;
+    for (int32_t x = 0; x < width; ++x) {
+      const uint8_t* p = row + x * cpp;
+      uchar4 t;
+      if (layout == BH_TEXEL_BGR8) t = make_uchar4(p[0], p[1], p[2], 255);
+      else if (layout == BH_TEXEL_RGB8) t = make_uchar4(p[2], p[1], p[0], 255);
+      else if (layout == BH_TEXEL_BGRA8) t = make_uchar4(p[0], p[1], p[2], p[3]);
+      else t = make_uchar4(p[2], p[1], p[0], p[3]);
+      host[size_t(y) * width + x] = t;
+    }
+  }
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  TexEntry e;
+  BH_CUDA(ctx, cudaMalloc(&e.texels, host.size() * sizeof(uchar4)));
+  cudaError_t ce = cudaMemcpy(e.texels, host.data(), host.size() * sizeof(uchar4), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    cudaFree(e.texels);
+    return cuda_err(ctx, ce, "texture upload");
+  }
+  e.width = width;
+  e.height = height;
+  e.alive = true;
+  for (size_t i = 0; i < ctx->textures.size(); ++i) {
+    if (!ctx->textures[i].alive && !ctx->textures[i].texels) {
+      ctx->textures[i] = e;
+      *out_id = int32_t(i);
+      return BH_OK;
+    }
+  }
+  ctx->textures.push_back(e);
+  *out_id = int32_t(ctx->textures.size() - 1);
+  return BH_OK;
+}
+
+int bh_texture_destroy(bh_ctx* ctx, int32_t id) {
+  if (!ctx) return BH_ERR_INVALID_ARGUMENT;
+  if (!texture_ok(ctx, id)) return set_err(ctx, BH_ERR_BAD_TEXTURE, "texture %d is not valid", id);
+  BH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->textures[id].texels);
+  ctx->textures[id] = TexEntry{};
+  return BH_OK;
+}
+
+int bh_render_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                     const bh_render_options* opts, void* stream) {
+  bh_render_options o;
+  int rc = check_inputs(ctx, scenes, n, frames, opts, &o);
+  if (rc) return rc;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return render_on_device(ctx, scenes, n, frames, o, st);
+}
+
+int bh_render(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+              const bh_render_options* opts) {
+  bh_render_options o;
+  int rc = check_inputs(ctx, scenes, n, frames, opts, &o);
+  if (rc) return rc;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  // device arena: pixels | classes | aux for every frame, 256-byte aligned
+  const int bpp = bytes_per_pixel(o.format);
+  std::vector<bh_frame> dframes(n);
+  std::vector<size_t> off_pix(n), off_cls(n), off_aux(n);
+  size_t total = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = total;
+    total += (bytes + 255) & ~size_t(255);
+    return at;
+  };
+  for (int i = 0; i < n; ++i) {
+    const size_t px = size_t(scenes[i].camera.width) * scenes[i].camera.height;
+    off_pix[i] = take(px * bpp);
+    off_cls[i] = frames[i].hit_class ? take(px) : 0;
+    off_aux[i] = frames[i].aux ? take(px * sizeof(float)) : 0;
+  }
+  if ((rc = ensure_dev(ctx, ctx->out_arena, total))) return rc;
+  uint8_t* base = ctx->out_arena.ptr;
+  for (int i = 0; i < n; ++i) {
+    dframes[i].pixels = base + off_pix[i];
+    dframes[i].hit_class = frames[i].hit_class ? base + off_cls[i] : nullptr;
+    dframes[i].aux = frames[i].aux ? reinterpret_cast<float*>(base + off_aux[i]) : nullptr;
+  }
+  if ((rc = render_on_device(ctx, scenes, n, dframes.data(), o, ctx->stream))) return rc;
+  // copy back, one cudaMemcpyAsync per buffer
+  for (int i = 0; i < n; ++i) {
+    const size_t px = size_t(scenes[i].camera.width) * scenes[i].camera.height;
+    ctx->d2h_bytes += px * bpp + (frames[i].hit_class ? px : 0) + (frames[i].aux ? px * sizeof(float) : 0);
+    BH_CUDA(ctx, cudaMemcpyAsync(frames[i].pixels, dframes[i].pixels, px * bpp, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    if (frames[i].hit_class)
+      BH_CUDA(ctx, cudaMemcpyAsync(frames[i].hit_class, dframes[i].hit_class, px, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    if (frames[i].aux)
+      BH_CUDA(ctx, cudaMemcpyAsync(frames[i].aux, dframes[i].aux, px * sizeof(float), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  }
+  BH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return bh_get_stats(ctx, &ctx->last);
+}
+
+int bh_get_stats(bh_ctx* ctx, bh_render_stats* out) {
+  if (!ctx || !out) return BH_ERR_INVALID_ARGUMENT;
+  if (!ctx->stats_valid) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "no render on this context yet");
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  BH_CUDA(ctx, cudaEventSynchronize(ctx->ev_stop));
+  BH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const DevCounters& c = *ctx->h_counters;
+  bh_render_stats s{};
+  s.rays = c.rays;
+  s.steps = c.steps;
+  s.band_rays = c.band_rays;
+  s.band_steps = c.band_steps;
+  s.band_overflow = c.band_overflow;
+  s.flags = c.flags;
+  float ms = 0;
+  BH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  s.kernel_ms = ms;
+  s.h2d_bytes = ctx->h2d_bytes;
+  s.d2h_bytes = ctx->d2h_bytes;
+  *out = s;
+  ctx->last = s;
+  return BH_OK;
+}
+
+// ---- sequences ------------------------------------------------------------------
+int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                       const bh_render_options* opts, bh_sequence** out) {
+  if (!out) return BH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  bh_render_options o;
+  int rc = check_inputs(ctx, scenes, n, frames, opts, &o);
+  if (rc) return rc;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  bh_sequence* q = new (std::nothrow) bh_sequence();
+  if (!q) return set_err(ctx, BH_ERR_OUT_OF_MEMORY, "sequence allocation");
+  q->ctx = ctx;
+  q->n = n;
+  q->opts = o;
+  q->scenes.assign(scenes, scenes + n);
+  q->frames.assign(frames, frames + n);
+  auto fail = [&](int code) {
+    bh_sequence_destroy(q);
+    return code;
+  };
+  cudaError_t e = cudaMallocHost(&q->h_scenes, sizeof(DevScene) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&q->d_scenes, sizeof(DevScene) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&q->d_counters, sizeof(DevCounters));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&q->ev_done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return fail(cuda_err(ctx, e, "sequence buffers"));
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    resolve_scene(ctx, scenes[i], frames[i], o, total, q->h_scenes + i);
+    total += padded_rays(scenes[i].camera);
+  }
+  LaunchParams p = base_params(o);
+  p.scenes = q->d_scenes;
+  p.n_scenes = n;
+  p.total_rays = total;
+  p.counters = q->d_counters;
+  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
+    q->band_capacity = band_capacity_for(total);
+    e = cudaMalloc(&q->band_list, sizeof(uint32_t) * q->band_capacity);
+    if (e != cudaSuccess) return fail(cuda_err(ctx, e, "band list"));
+    p.band_list = q->band_list;
+    p.band_capacity = q->band_capacity;
+  }
+  int blocks = 0;
+  if (o.schedule == BH_SCHEDULE_PERSISTENT && (rc = persistent_blocks(ctx, p, o, &blocks))) return fail(rc);
+  cudaStream_t cs = nullptr;
+  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(cuda_err(ctx, e, "capture stream"));
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(q->d_scenes, q->h_scenes, sizeof(DevScene) * n, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(q->d_counters, 0, sizeof(DevCounters), cs);
+  if (e == cudaSuccess) {
+    if (o.schedule == BH_SCHEDULE_GRID) {
+      std::vector<int32_t> w(n), h(n);
+      for (int i = 0; i < n; ++i) {
+        w[i] = scenes[i].camera.width;
+        h[i] = scenes[i].camera.height;
+      }
+      e = bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, cs);
+    } else {
+      e = bhgb::launch_persistent(p, o.threads_per_block, blocks, cs);
+    }
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+  cudaStreamDestroy(cs);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(cuda_err(ctx, e, "sequence capture"));
+  }
+  q->graph = g;
+  e = cudaGraphInstantiate(&q->exec, g, 0);
+  if (e != cudaSuccess) return fail(cuda_err(ctx, e, "graph instantiate"));
+  *out = q;
+  return BH_OK;
+}
+
+int bh_sequence_update(bh_sequence* q, const bh_scene* scenes, int32_t n) {
+  if (!q || !scenes) return BH_ERR_INVALID_ARGUMENT;
+  bh_ctx* ctx = q->ctx;
+  if (n != q->n) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "sequence holds %d scenes, got %d", q->n, n);
+  for (int i = 0; i < n; ++i) {
+    const bh_scene& a = scenes[i];
+    const bh_scene& b = q->scenes[i];
+    if (a.camera.width != b.camera.width || a.camera.height != b.camera.height ||
+        a.background != b.background || a.disc.enabled != b.disc.enabled ||
+        (a.disc.enabled && a.disc.texture != b.disc.texture))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d changes sizes or textures of the sequence", i);
+    int rc = validate_scene(ctx, a, i, q->opts);
+    if (rc) return rc;
+  }
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (q->launched) BH_CUDA(ctx, cudaEventSynchronize(q->ev_done));
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    resolve_scene(ctx, scenes[i], q->frames[i], q->opts, total, q->h_scenes + i);
+    total += padded_rays(scenes[i].camera);
+    q->scenes[i] = scenes[i];
+  }
+  return BH_OK;
+}
+
+int bh_sequence_launch(bh_sequence* q, void* stream) {
+  if (!q) return BH_ERR_INVALID_ARGUMENT;
+  bh_ctx* ctx = q->ctx;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  BH_CUDA(ctx, cudaGraphLaunch(q->exec, st));
+  BH_CUDA(ctx, cudaEventRecord(q->ev_done, st));
+  q->launched = true;
+  return BH_OK;
+}
+
+int bh_sequence_stats(bh_sequence* q, bh_render_stats* out) {
+  if (!q || !out) return BH_ERR_INVALID_ARGUMENT;
+  bh_ctx* ctx = q->ctx;
+  if (!q->launched) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "sequence not launched yet");
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  BH_CUDA(ctx, cudaEventSynchronize(q->ev_done));
+  DevCounters c;
+  BH_CUDA(ctx, cudaMemcpy(&c, q->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+  bh_render_stats s{};
+  s.rays = c.rays;
+  s.steps = c.steps;
+  s.band_rays = c.band_rays;
+  s.band_steps = c.band_steps;
+  s.band_overflow = c.band_overflow;
+  s.flags = c.flags;
+  *out = s;
+  return BH_OK;
+}
+
+void bh_sequence_destroy(bh_sequence* q) {
+  if (!q) return;
+  if (q->ctx) cudaSetDevice(q->ctx->device);
+  if (q->launched && q->ev_done) cudaEventSynchronize(q->ev_done);
+  if (q->exec) cudaGraphExecDestroy(q->exec);
+  if (q->graph) cudaGraphDestroy(q->graph);
+  if (q->h_scenes) cudaFreeHost(q->h_scenes);
+  if (q->d_scenes) cudaFree(q->d_scenes);
+  if (q->d_counters) cudaFree(q->d_counters);
+  if (q->band_list) cudaFree(q->band_list);
+  if (q->ev_done) cudaEventDestroy(q->ev_done);
+  delete q;
+}
+
+// ---- probes ----------------------------------------------------------------------
+int bh_probe_fp32_peak(bh_ctx* ctx, double* tflops, int32_t* sm_count) {
+  if (!ctx || !tflops) return BH_ERR_INVALID_ARGUMENT;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  float* sink = nullptr;
+  BH_CUDA(ctx, cudaMalloc(&sink, sizeof(float) * 65536));
+  const int threads = 256, blocks = ctx->sm_count * 8, iters = 4096;
+  double best = 0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(ctx->ev_start, ctx->stream);
+    cudaError_t e = bhgb::launch_fp32_probe(sink, blocks, threads, iters, ctx->stream);
+    cudaEventRecord(ctx->ev_stop, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_stop);
+    if (e != cudaSuccess) {
+      cudaFree(sink);
+      return cuda_err(ctx, e, "fp32 probe");
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
+    const double flops = double(blocks) * threads * iters * 16 * 8 * 2;
+    if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaFree(sink);
+  *tflops = best;
+  if (sm_count) *sm_count = ctx->sm_count;
+  return BH_OK;
+}
+
+int bh_probe_fp64_peak(bh_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return BH_ERR_INVALID_ARGUMENT;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  double* sink = nullptr;
+  BH_CUDA(ctx, cudaMalloc(&sink, sizeof(double) * 65536));
+  const int threads = 256, blocks = ctx->sm_count * 4, iters = 64;
+  double best = 0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(ctx->ev_start, ctx->stream);
+    cudaError_t e = bhgb::launch_fp64_probe(sink, blocks, threads, iters, ctx->stream);
+    cudaEventRecord(ctx->ev_stop, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_stop);
+    if (e != cudaSuccess) {
+      cudaFree(sink);
+      return cuda_err(ctx, e, "fp64 probe");
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
+    const double flops = double(blocks) * threads * iters * 8 * 4 * 2;
+    if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaFree(sink);
+  *tflops = best;
+  return BH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+// Internal types shared by the kernels (bh_kernels.cu) and the C ABI
+// (bh_capi.cu). Nothing here is part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bh_gb300.h"
+
+namespace bhgb {
+
+// Texture resident in device memory, texels stored as BGRA8 (uchar4.x = B).
+struct DevTexture {
+  const uchar4* texels;
+  int32_t width;
+  int32_t height;
+};
+
+// One scene resolved for the device. Positions are relative to the hole.
+// The FP64 block drives the FP64 paths; the FP32 block is the same data
+// rounded once on the host.
+//
+// Ray generation (camera.h:55-59, blackhole_solution_test.cc:167-170): the
+// reference's pv = focus_vector - vy*(W/2 - x) - vz*(H/2 - y) - hole and
+// yv = normalize(F - pv). With E0 = F - pv(W/2, H/2) this is
+// yv = normalize(E0 + vy*(W/2 - x) + vz*(H/2 - y)).
+struct DevScene {
+  double F[3];    // camera focus
+  double E0[3];   // F - pv at the image centre (REF) or -focus_vector (PINHOLE)
+  double vy[3];
+  double vz[3];
+  double dc[3];   // disc centre
+  double dn[3];   // disc normal (fixed at construction, vector_object.h:325)
+  double dv1[3];  // quad corner vertex()[1]
+  double ds1[3];  // vertex()[2] - vertex()[1]
+  double ds2[3];  // vertex()[4] - vertex()[1]
+  double de1[3];  // polar basis e1 = s1 / |s1|
+  double de2[3];  // polar basis e2 = n x e1
+  double mass, b_c, r_h;      // M, 3 sqrt(3) M, 2 M
+  double r_in, r_out;
+  double s1_len, s2_len;
+  double half_w, half_h;      // W / 2.0, H / 2.0
+
+  float F_f[3], E0_f[3], vy_f[3], vz_f[3];
+  float dc_f[3], dn_f[3], dv1_f[3], ds1_f[3], ds2_f[3], de1_f[3], de2_f[3];
+  float mass_f, b_c_f, r_h_f, r_in_f, r_out_f, s1_len_f, s2_len_f, half_w_f, half_h_f;
+
+  DevTexture disc_tex;
+  DevTexture bg_tex;
+  int32_t width, height;
+  int32_t disc_on, disc_map, has_bg;
+  int32_t tiles_x;            // ceil(W / 8): persistent schedule, 8x4 tiles
+  int64_t ray_begin;          // first ray index of this scene (persistent)
+  uint8_t* pixels;
+  uint8_t* cls;
+  float* aux;
+};
+
+// Device-side counters of one render (reset before every render).
+struct DevCounters {
+  unsigned long long next_ray;      // persistent work queue head
+  unsigned long long band_count;    // entries appended to the band list
+  unsigned long long band_next;     // band work queue head
+  unsigned long long steps;
+  unsigned long long band_steps;
+  unsigned long long band_rays;
+  unsigned long long band_overflow;
+  unsigned long long rays;
+  unsigned long long flags;
+  unsigned long long pad[7];
+};
+
+enum : unsigned long long {
+  kFlagBandQueueFull = 1ull << 0,
+};
+
+struct LaunchParams {
+  const DevScene* scenes;
+  int32_t n_scenes;
+  int32_t integrator;
+  int32_t precision;
+  int32_t format;
+  int32_t raygen;
+  int32_t max_steps;
+  double step;
+  double u_escape;            // M / r_escape
+  double band;                // |b - b_c| / M below which MIXED goes FP64
+  int64_t total_rays;         // persistent: sum of padded scene ray counts
+  DevCounters* counters;
+  uint32_t* band_list;        // persistent MIXED: deferred band rays
+  uint32_t band_capacity;
+  int32_t refill_threshold;
+};
+
+// Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.
+cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
+                        int block_x, int block_y, cudaStream_t stream);
+cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream);
+cudaError_t persistent_occupancy(const LaunchParams& p, int threads, int* blocks_per_sm);
+cudaError_t launch_fp32_probe(float* sink, int blocks, int threads, int iters, cudaStream_t stream);
+cudaError_t launch_fp64_probe(double* sink, int blocks, int threads, int iters, cudaStream_t stream);
+
+}  // namespace bhgb

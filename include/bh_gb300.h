@@ -1,0 +1,235 @@
+/*
+ * bh_gb300.h -- C ABI of the GB300 (sm_103a) geodesic ray tracer.
+ *
+ * This is the drop-in boundary for the per-pixel Schwarzschild geodesic render
+ * of lackhole/blackhole_8. In the reference that render is not a library call:
+ * it is the body of the frame loop in
+ * include/blackhole/blackhole_solution_test.cc:161-298, fed by
+ *   - Camera<double>            (camera.h:21-71)
+ *   - StaticBlackhole<double>   (blackhole_solution.h:16-96)
+ *   - Annulus<double> + texture (object/vector_object.h:306-356,
+ *                                object/material.h:29-35)
+ *   - ObjectManager<double>     (object/object_manager.h:69-85)
+ * and it writes a CV_8UC3 (BGR) cv::Mat (blackhole_solution_test.cc:117,
+ * 214, 229-233). This header replaces that loop with plain C entry points:
+ * scenes are POD structs of resolved world-space poses, textures are uploaded
+ * once, frames are written to caller-owned buffers.
+ *
+ * Conventions
+ *   - Every function returns an int status: BH_OK (0) or a negative BH_ERR_*;
+ *     bh_last_error() gives the message. Nothing aborts the process (the
+ *     reference calls std::terminate on an empty texture, material.h:30-33).
+ *   - The caller owns every host buffer. Textures are copied at upload.
+ *   - One context = one CUDA device + one CUDA stream. A context is not
+ *     re-entrant: use one per host thread.
+ *   - Lengths are world units; angles are radians.
+ */
+#ifndef BH_GB300_H_
+#define BH_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BH_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  BH_OK = 0,
+  BH_ERR_INVALID_ARGUMENT = -1,
+  BH_ERR_EMPTY_TEXTURE = -2,
+  BH_ERR_BAD_TEXTURE = -3,
+  BH_ERR_CUDA = -4,
+  BH_ERR_OUT_OF_MEMORY = -5,
+  BH_ERR_UNSUPPORTED = -6,
+  BH_ERR_TIMEOUT = -7,
+  BH_ERR_NO_DEVICE = -8,
+  BH_ERR_DEVICE_FAULT = -9
+};
+
+/* ---- enumerations --------------------------------------------------------- */
+/* Integrator. REF_TRAPEZOID is the reference's own scheme: dphi/du = 1/sqrt(G)
+ * by a 20+20-segment trapezoid rule in u with straight-chord collision tests
+ * (blackhole_solution_test.cc:185-296). RK4 integrates u'' = -u + 3 M u^2 in
+ * phi with a fixed step and exact horizon / escape / disc-plane events. */
+enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1 };
+
+/* Arithmetic. MIXED (RK4 only): FP32 bulk, FP64 for rays whose impact
+ * parameter lies within `band` of 3*sqrt(3)*M, FP64 disc-crossing refinement. */
+enum { BH_PRECISION_FP32 = 0, BH_PRECISION_FP64 = 1, BH_PRECISION_MIXED = 2 };
+
+/* Ray generation. REF reproduces the reference: the ray runs from the focus
+ * toward the point Camera::PixelVector(x, y) (a direction, camera.h:55-59,
+ * used as a point at blackhole_solution_test.cc:167-170). PINHOLE runs it
+ * along PixelVector(x, y) from the focus. */
+enum { BH_RAYGEN_REF = 0, BH_RAYGEN_PINHOLE = 1 };
+
+/* Disc texture mapping. REF_PLANAR is Rectangle::color (vector_object.h:
+ * 159-179): nearest texel on the quad basis s1 = v2 - v1, s2 = v4 - v1.
+ * POLAR: x = (r - r_inner) / (r_outer - r_inner), y = azimuth / 2pi about
+ * e1 = s1/|s1|, e2 = normal x e1. */
+enum { BH_DISC_MAP_REF_PLANAR = 0, BH_DISC_MAP_POLAR = 1 };
+
+/* Framebuffer formats. BGR8 is the reference's CV_8UC3 layout. */
+enum { BH_FORMAT_BGRA8 = 0, BH_FORMAT_BGR8 = 1, BH_FORMAT_RGBA8 = 2 };
+
+/* Texture layouts accepted by bh_texture_create. BGR8 is cv::Mat CV_8UC3. */
+enum { BH_TEXEL_BGR8 = 0, BH_TEXEL_RGB8 = 1, BH_TEXEL_BGRA8 = 2, BH_TEXEL_RGBA8 = 3 };
+
+/* Work schedule. GRID: one thread per pixel over a 2-D grid per frame.
+ * PERSISTENT: one work-stealing launch over every frame of the call, warps
+ * refill finished lanes with new rays; FP64 band rays are deferred to a
+ * second persistent pass. */
+enum { BH_SCHEDULE_GRID = 0, BH_SCHEDULE_PERSISTENT = 1 };
+
+/* Per-pixel hit classes written to bh_frame.hit_class. */
+enum { BH_CLASS_MISS = 0, BH_CLASS_HORIZON = 1, BH_CLASS_DISC = 2, BH_CLASS_MAXSTEPS = 3 };
+
+/* ---- scene ------------------------------------------------------------------ */
+/* Camera<T> state (camera.h:21-71 on Object<T>, object/object.h:23-118). */
+typedef struct bh_camera {
+  double position[3];  /* focus() = Object::position() */
+  double axis_x[3];    /* vector_x(): viewing direction */
+  double axis_y[3];    /* vector_y(): +x image direction */
+  double axis_z[3];    /* vector_z(): +y image direction */
+  double focus_len;    /* width / (2 tan(fov/2)), camera.h:37-41 */
+  int32_t width;
+  int32_t height;
+} bh_camera;
+
+/* StaticBlackhole<T> (blackhole_solution.h:24-25). */
+typedef struct bh_hole {
+  double position[3];
+  double mass;
+} bh_hole;
+
+/* Annulus<T> (vector_object.h:306-356) and its texture. */
+typedef struct bh_disc {
+  double center[3];    /* vertex()[0] */
+  double normal[3];    /* norm_: fixed at construction, vector_object.h:325 */
+  double corner[3];    /* vertex()[1] */
+  double edge_s1[3];   /* vertex()[2] - vertex()[1] */
+  double edge_s2[3];   /* vertex()[4] - vertex()[1] */
+  double r_inner;
+  double r_outer;
+  int32_t texture;     /* id from bh_texture_create; must be valid if enabled */
+  int32_t mapping;     /* BH_DISC_MAP_* */
+  int32_t enabled;     /* 0: scene has no disc */
+  int32_t reserved;
+} bh_disc;
+
+typedef struct bh_scene {
+  bh_camera camera;
+  bh_hole hole;
+  bh_disc disc;
+  int32_t background;  /* equirectangular texture id, or -1: escaped rays stay
+                          black as in the reference (screen is zeroed,
+                          blackhole_solution_test.cc:140) */
+  int32_t reserved;
+} bh_scene;
+
+/* One output frame; width and height come from the scene's camera. */
+typedef struct bh_frame {
+  void* pixels;        /* width*height*bytes_per_pixel(format), row-major */
+  uint8_t* hit_class;  /* optional (NULL): width*height BH_CLASS_* */
+  float* aux;          /* optional (NULL): width*height. RK4 only: deflection
+                          angle (rad) of escaped rays, hit radius (units of M)
+                          of disc hits, 0 otherwise */
+} bh_frame;
+
+typedef struct bh_render_options {
+  int32_t integrator;        /* BH_INTEGRATOR_* (default RK4) */
+  int32_t precision;         /* BH_PRECISION_* (default FP32) */
+  int32_t raygen;            /* BH_RAYGEN_* (default REF) */
+  int32_t format;            /* BH_FORMAT_* (default BGRA8) */
+  int32_t schedule;          /* BH_SCHEDULE_* (default GRID) */
+  int32_t max_steps;         /* RK4 step cap (default 4000) */
+  double step;               /* RK4 step in phi (default 0.01) */
+  double r_escape;           /* RK4 escape radius in units of M (default 100) */
+  double band;               /* MIXED: FP64 band half-width of |b - 3 sqrt(3) M|
+                                in units of M (default 0.01) */
+  int32_t block_x;           /* GRID block shape (default 32 x 4) */
+  int32_t block_y;
+  int32_t threads_per_block; /* PERSISTENT block size (default 256) */
+  int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
+  int32_t refill_threshold;  /* PERSISTENT: refill a warp once this many lanes
+                                are idle (default 8) */
+  int32_t reserved[9];
+} bh_render_options;
+
+/* Counters of the most recent render on a context. */
+typedef struct bh_render_stats {
+  uint64_t rays;          /* pixels traced */
+  uint64_t steps;         /* integration steps summed over rays */
+  uint64_t band_rays;     /* rays traced in FP64 because of the band */
+  uint64_t band_steps;    /* steps of those rays */
+  uint64_t band_overflow; /* band rays traced inline (deferral list full) */
+  uint64_t flags;         /* device error bits (0 = none) */
+  double kernel_ms;       /* device time of the launches, CUDA events */
+  uint64_t h2d_bytes;     /* bytes copied host -> device by the call */
+  uint64_t d2h_bytes;     /* bytes copied device -> host by the call
+                             (frames; the 128-byte counters excluded) */
+} bh_render_stats;
+
+typedef struct bh_ctx bh_ctx;
+typedef struct bh_sequence bh_sequence;
+
+/* ---- context ---------------------------------------------------------------- */
+int bh_abi_version(void);
+void bh_default_options(bh_render_options* opts);
+int bh_create(bh_ctx** out, int device);
+void bh_destroy(bh_ctx* ctx);
+const char* bh_last_error(const bh_ctx* ctx);
+/* Stream used by the context (a cudaStream_t). */
+void* bh_stream(bh_ctx* ctx);
+
+/* ---- textures (Material<T>::SetTexture, material.h:29-35) --------------------
+ * Copies a width x height texture to the device. An empty texture returns
+ * BH_ERR_EMPTY_TEXTURE where the reference terminates. row_stride in bytes
+ * (0 = packed). */
+int bh_texture_create(bh_ctx* ctx, const uint8_t* texels, int32_t width, int32_t height,
+                      int32_t layout, int64_t row_stride, int32_t* out_id);
+int bh_texture_destroy(bh_ctx* ctx, int32_t id);
+
+/* ---- render ---------------------------------------------------------------
+ * Replaces the frame body blackhole_solution_test.cc:161-298 for n scenes.
+ * bh_render: host frames; uploads the scenes, renders, copies the frames back
+ * and returns when they are in host memory.
+ * bh_render_device: frames in device memory; enqueued on `stream` (a
+ * cudaStream_t, NULL = the context's stream) and returns without waiting. */
+int bh_render(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+              const bh_render_options* opts);
+int bh_render_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                     const bh_render_options* opts, void* stream);
+/* Waits for the context's work and returns the counters of the last render. */
+int bh_get_stats(bh_ctx* ctx, bh_render_stats* out);
+
+/* ---- captured sequences (camera fly-through as one CUDA graph) --------------
+ * Captures the render of n scenes into device frames as a CUDA graph. The
+ * scenes can be replaced between launches (same count, sizes and textures);
+ * the new poses are copied into the graph's own device buffer by the launch.*/
+int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                       const bh_render_options* opts, bh_sequence** out);
+int bh_sequence_update(bh_sequence* seq, const bh_scene* scenes, int32_t n);
+int bh_sequence_launch(bh_sequence* seq, void* stream);
+/* Waits for the last launch of the sequence and returns its counters
+ * (kernel_ms is not measured for sequences and reads 0). */
+int bh_sequence_stats(bh_sequence* seq, bh_render_stats* out);
+void bh_sequence_destroy(bh_sequence* seq);
+
+/* ---- device probes ------------------------------------------------------------
+ * Measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops) and its
+ * multiprocessor count; used as the roofline denominator. */
+int bh_probe_fp32_peak(bh_ctx* ctx, double* tflops, int32_t* sm_count);
+int bh_probe_fp64_peak(bh_ctx* ctx, double* tflops);
+
+/* Algorithmic FP32 flops of one RK4 step of the tracer (FMA = 2). */
+#define BH_RK4_FLOPS_PER_STEP 36
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BH_GB300_H_ */

@@ -1,0 +1,294 @@
+"""GPU parity: the sm_103a tracer through the C ABI against the FP64 oracle
+and against the reference's own render (golden fixtures).
+
+Bars (the tolerances are written in each test):
+- trapezoid (reference scheme), FP64: hit classes equal to the reference's
+  except on class boundaries; colours equal except where a texel-edge tie
+  rounds the other way.
+- RK4 FP64: classes and deflections equal to the FP64 oracle to rounding.
+- RK4 FP32 / MIXED: hit class agrees on >= 99.9 % of pixels and the rest lie
+  on class boundaries; colour within 1 LSB away from texel and disc edges;
+  deflection within 1e-4 rad of the FP64 oracle (MIXED: every escaped ray;
+  FP32: rays outside the band around 3 sqrt(3) M).
+"""
+import ctypes as C
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import helpers
+from blackhole_8_gb300 import capi
+from blackhole_8_gb300 import scene as S
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = json.load(open(os.path.join(GOLDEN, "index.json")))["cases"]
+B_C = 3.0 * math.sqrt(3.0)
+
+
+def opts(**kw):
+    return capi.default_options(**kw)
+
+
+def dilate(mask, n=1):
+    m = mask.copy()
+    for _ in range(n):
+        m2 = m.copy()
+        m2[1:, :] |= m[:-1, :]
+        m2[:-1, :] |= m[1:, :]
+        m2[:, 1:] |= m[:, :-1]
+        m2[:, :-1] |= m[:, 1:]
+        m = m2
+    return m
+
+
+# ---------------------------------------------------------------------------
+# the reference's trapezoid scheme
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["file"])
+def test_trapezoid_fp64_matches_reference(renderer, case):
+    sc = helpers.build(case["builder"], case["width"], case["height"])
+    g = np.load(os.path.join(GOLDEN, case["file"]))
+    o = opts(integrator=capi.INTEGRATOR_REF_TRAPEZOID, precision=capi.PRECISION_FP64, format=capi.FORMAT_BGR8)
+    out = renderer.render([sc], o, hit_class=True)[0]
+    bad = out.hit_class != g["cls"]
+    assert bad.mean() <= 1e-3 and not (bad & ~dilate(helpers.class_boundary_mask(g["cls"]))).any()
+    diff = (out.pixels != g["bgr"]).any(-1)
+    assert diff.mean() <= 2e-3, f"{diff.sum()} pixels differ"
+
+
+def test_trapezoid_fp32_matches_oracle(renderer):
+    sc = helpers.cfg0_planar(160, 90)
+    ref = oracle.render_ref(sc)
+    o = opts(integrator=capi.INTEGRATOR_REF_TRAPEZOID, precision=capi.PRECISION_FP32)
+    out = renderer.render([sc], o, hit_class=True)[0]
+    bad = out.hit_class != ref["cls"]
+    assert bad.mean() <= 5e-3
+    assert not (bad & ~dilate(helpers.class_boundary_mask(ref["cls"]), 2)).any()
+
+
+# ---------------------------------------------------------------------------
+# RK4
+@pytest.fixture(scope="module")
+def single():
+    sc = S.single_scene(320, 180)
+    return sc, oracle.render_rk4(sc)
+
+
+def boundary_pixels(o, band=0.05, tex=0.02, edge=2e-3):
+    """Pixels whose result may flip under rounding: next to another class,
+    near a disc edge, near the critical impact parameter or near a texel
+    edge."""
+    m = dilate(helpers.class_boundary_mask(o["cls"]))
+    m |= (o["cls"] == capi.CLASS_DISC) & (o["margin_r"] < edge)
+    m |= np.abs(o["b_over_m"] - B_C) < band
+    m |= o["margin_tex"] < tex
+    return m
+
+
+def compare(out, o, boundary, aux_tol, colour_lsb=1):
+    cls_ok = out.hit_class == o["cls"]
+    assert cls_ok.mean() >= 0.999, f"class agreement {cls_ok.mean():.5f}"
+    assert not (~cls_ok & ~boundary).any(), "class mismatch away from boundaries"
+    strict = cls_ok & ~boundary
+    dcol = np.abs(out.pixels[..., :3].astype(int) - o["bgra"][..., :3].astype(int)).max(-1)
+    assert dcol[strict].max(initial=0) <= colour_lsb
+    esc = strict & (o["cls"] == capi.CLASS_MISS)
+    dsk = strict & (o["cls"] == capi.CLASS_DISC)
+    err_esc = np.abs(out.aux[esc] - o["aux"][esc]).max(initial=0)
+    err_dsk = np.abs(out.aux[dsk] - o["aux"][dsk]).max(initial=0)
+    assert err_esc <= aux_tol, f"deflection error {err_esc}"
+    assert err_dsk <= max(aux_tol, 1e-3), f"hit radius error {err_dsk}"
+    return err_esc, err_dsk
+
+
+def test_rk4_fp64_matches_oracle(renderer, single):
+    sc, o = single
+    out = renderer.render([sc], opts(precision=capi.PRECISION_FP64), hit_class=True, aux=True)[0]
+    boundary = boundary_pixels(o, band=1e-6, tex=1e-6, edge=1e-9)
+    e1, e2 = compare(out, o, boundary, aux_tol=1e-6)
+    assert (out.hit_class == o["cls"]).mean() >= 0.9999
+
+
+def test_rk4_fp32_matches_oracle(renderer, single):
+    sc, o = single
+    out = renderer.render([sc], opts(precision=capi.PRECISION_FP32), hit_class=True, aux=True)[0]
+    compare(out, o, boundary_pixels(o), aux_tol=1e-4)
+
+
+@pytest.mark.parametrize("schedule", [capi.SCHEDULE_GRID, capi.SCHEDULE_PERSISTENT])
+def test_rk4_mixed_meets_bound_on_every_escaped_ray(renderer, single, schedule):
+    sc, o = single
+    out = renderer.render([sc], opts(precision=capi.PRECISION_MIXED, schedule=schedule), hit_class=True,
+                          aux=True)[0]
+    st = renderer.stats()
+    assert st.rays == 320 * 180
+    assert st.band_rays > 0 and st.band_overflow == 0
+    # near the critical impact parameter only the class itself may flip
+    compare(out, o, boundary_pixels(o, band=1e-4), aux_tol=1e-4)
+
+
+def test_persistent_matches_grid(renderer, single):
+    sc, _ = single
+    a = renderer.render([sc], opts(schedule=capi.SCHEDULE_GRID), hit_class=True, aux=True)[0]
+    sa = renderer.stats()
+    b = renderer.render([sc], opts(schedule=capi.SCHEDULE_PERSISTENT), hit_class=True, aux=True)[0]
+    sb = renderer.stats()
+    assert np.array_equal(a.hit_class, b.hit_class)
+    assert (a.pixels != b.pixels).any(-1).mean() <= 1e-4
+    assert np.abs(a.aux - b.aux).max() <= 1e-5
+    assert sa.steps == sb.steps and sa.rays == sb.rays
+
+
+def test_step_counts_match_oracle(renderer):
+    sc = S.single_scene(96, 54)
+    o = oracle.render_rk4(sc)
+    renderer.render([sc], opts(precision=capi.PRECISION_FP64))
+    st = renderer.stats()
+    assert st.rays == 96 * 54
+    assert abs(int(st.steps) - int(o["steps"].sum())) <= 2
+
+
+def test_pixel_formats_agree(renderer):
+    sc = S.single_scene(64, 36)
+    a = renderer.render([sc], opts(format=capi.FORMAT_BGRA8))[0].pixels
+    b = renderer.render([sc], opts(format=capi.FORMAT_BGR8))[0].pixels
+    c = renderer.render([sc], opts(format=capi.FORMAT_RGBA8))[0].pixels
+    assert np.array_equal(a[..., :3], b)
+    assert np.array_equal(a[..., 2::-1], c[..., :3])
+    assert (a[..., 3] == 255).all()
+
+
+def test_pinhole_raygen_differs_from_ref(renderer):
+    sc = S.single_scene(64, 36)
+    a = renderer.render([sc], opts(raygen=capi.RAYGEN_REF), hit_class=True)[0].hit_class
+    b = renderer.render([sc], opts(raygen=capi.RAYGEN_PINHOLE), hit_class=True)[0].hit_class
+    assert (a != b).any()
+
+
+def test_full_hd_frames_sampled_against_oracle(renderer):
+    """Full-size 1920x1080 fly-through frames; a seeded pixel sample of each is
+    checked against the FP64 oracle."""
+    scenes = S.flythrough(120)
+    picks = [scenes[0], scenes[60], scenes[119]]
+    out = renderer.render(picks, opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT),
+                          hit_class=True, aux=True)
+    rng = np.random.default_rng(11)
+    for sc, fb in zip(picks, out):
+        xs = rng.integers(0, 1920, 3000)
+        ys = rng.integers(0, 1080, 3000)
+        o = oracle.render_rk4(sc, pixels=np.stack([xs, ys], 1))
+        cls = fb.hit_class[ys, xs]
+        agree = cls == o["cls"]
+        assert agree.mean() >= 0.998
+        esc = agree & (o["cls"] == capi.CLASS_MISS)
+        assert np.abs(fb.aux[ys, xs][esc] - o["aux"][esc]).max() <= 1e-4
+
+
+def test_batched_uneven_scenes(renderer):
+    scenes = S.batched_scenes(12, seed=3, min_side=32, max_side=160, bg_size=(256, 128))
+    out = renderer.render(scenes, opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT),
+                          hit_class=True, aux=True)
+    st = renderer.stats()
+    assert st.rays == sum(s.camera.width() * s.camera.height() for s in scenes)
+    for sc, fb in zip(scenes, out):
+        o = oracle.render_rk4(sc)
+        agree = fb.hit_class == o["cls"]
+        assert agree.mean() >= 0.995, sc.meta
+        esc = agree & (o["cls"] == capi.CLASS_MISS)
+        assert np.abs(fb.aux[esc] - o["aux"][esc]).max(initial=0) <= 1e-4
+
+
+# ---------------------------------------------------------------------------
+# device buffers and captured sequences
+def _device_frames(torch, scenes, with_cls=True):
+    bufs, frames = [], (capi.Frame * len(scenes))()
+    for i, s in enumerate(scenes):
+        px = torch.zeros((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
+        cl = torch.zeros((s.camera.height(), s.camera.width()), dtype=torch.uint8, device="cuda")
+        bufs.append((px, cl))
+        frames[i].pixels = px.data_ptr()
+        frames[i].hit_class = cl.data_ptr() if with_cls else None
+        frames[i].aux = None
+    return bufs, frames
+
+
+def test_sequence_graph_matches_direct_render(renderer):
+    torch = pytest.importorskip("torch")
+    scenes = S.flythrough(6, 96, 54)
+    o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
+    bufs, frames = _device_frames(torch, scenes)
+    seq = renderer.sequence(renderer.c_scenes(scenes), frames, o)
+    seq.launch()
+    torch.cuda.synchronize()
+    renderer.stats()
+    direct = renderer.render(scenes, o, hit_class=True)
+    for (px, cl), d in zip(bufs, direct):
+        assert np.array_equal(px.cpu().numpy(), d.pixels)
+        assert np.array_equal(cl.cpu().numpy(), d.hit_class)
+    # new poses, same sizes: update and replay
+    later = S.flythrough(12, 96, 54)[6:]
+    seq.update(renderer.c_scenes(later))
+    seq.launch()
+    torch.cuda.synchronize()
+    direct = renderer.render(later, o, hit_class=True)
+    for (px, cl), d in zip(bufs, direct):
+        assert np.array_equal(px.cpu().numpy(), d.pixels)
+    seq.close()
+
+
+def test_render_device_on_torch_stream(renderer):
+    torch = pytest.importorskip("torch")
+    scenes = [S.single_scene(64, 36)]
+    bufs, frames = _device_frames(torch, scenes)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        renderer.render_device(renderer.c_scenes(scenes), frames, opts(), stream=st.cuda_stream)
+    st.synchronize()
+    ref = renderer.render(scenes, opts())[0]
+    assert np.array_equal(bufs[0][0].cpu().numpy(), ref.pixels)
+
+
+# ---------------------------------------------------------------------------
+# error paths (no GPU fault involved)
+def test_error_paths(renderer):
+    lib, ctx = renderer.lib, renderer.ctx
+    out = C.c_int32()
+    empty = np.zeros((0, 0, 3), np.uint8)
+    assert lib.bh_texture_create(ctx, None, 0, 0, capi.TEXEL_BGR8, 0, C.byref(out)) == capi.BH_ERR_EMPTY_TEXTURE
+    assert b"empty" in lib.bh_last_error(ctx)
+    sc = S.single_scene(32, 18)
+    cs = renderer.c_scenes([sc])
+    frames = (capi.Frame * 1)()
+    buf = np.zeros((18, 32, 4), np.uint8)
+    frames[0].pixels = buf.ctypes.data
+    # bad texture id
+    bad = renderer.c_scenes([sc])
+    bad[0].disc.texture = 999
+    assert lib.bh_render(ctx, bad, 1, frames, C.byref(opts())) == capi.BH_ERR_BAD_TEXTURE
+    # disc plane not through the hole: the RK4 events need it
+    off = renderer.c_scenes([sc])
+    off[0].disc.center[2] = 0.5
+    assert lib.bh_render(ctx, off, 1, frames, C.byref(opts())) == capi.BH_ERR_UNSUPPORTED
+    # ... while the reference scheme handles any disc placement
+    o = opts(integrator=capi.INTEGRATOR_REF_TRAPEZOID)
+    assert lib.bh_render(ctx, off, 1, frames, C.byref(o)) == capi.BH_OK
+    # camera outside the escape radius
+    far = renderer.c_scenes([sc])
+    far[0].camera.position[0] = -150.0
+    assert lib.bh_render(ctx, far, 1, frames, C.byref(opts())) == capi.BH_ERR_UNSUPPORTED
+    # invalid options
+    for kw in ({"step": 0.0 - 1}, {"max_steps": -1}, {"block_x": 7, "block_y": 1}, {"precision": 9},
+               {"integrator": capi.INTEGRATOR_REF_TRAPEZOID, "precision": capi.PRECISION_MIXED}):
+        assert lib.bh_render(ctx, cs, 1, frames, C.byref(opts(**kw))) in (capi.BH_ERR_INVALID_ARGUMENT,
+                                                                          capi.BH_ERR_UNSUPPORTED)
+    # non-finite camera
+    nan = renderer.c_scenes([sc])
+    nan[0].camera.axis_x[0] = float("nan")
+    assert lib.bh_render(ctx, nan, 1, frames, C.byref(opts())) == capi.BH_ERR_INVALID_ARGUMENT
+    # the context still renders after the errors
+    assert lib.bh_render(ctx, cs, 1, frames, C.byref(opts())) == capi.BH_OK
