@@ -65,7 +65,8 @@ class RenderOptions(C.Structure):
                 ("step", C.c_double), ("r_escape", C.c_double), ("band", C.c_double),
                 ("block_x", C.c_int32), ("block_y", C.c_int32), ("threads_per_block", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("refill_threshold", C.c_int32),
-                ("reserved", C.c_int32 * 9)]
+                ("band_step", C.c_double), ("setup_band", C.c_double), ("slice_steps", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class RenderStats(C.Structure):

@@ -1,0 +1,103 @@
+"""Headless renderer: the reference's interactive frame loop
+(blackhole_solution_test.cc:153-407: render, HUD, VideoWriter, imshow)
+without a window. Renders one of the synthetic workloads on the GPU, keeps
+frames on the device, optionally copies them out as binary PPM files, and
+prints one JSON line of timings.
+
+    python -m blackhole_8_gb300.cli --workload flythrough --frames 8 \
+        --precision fp32 --schedule grid --repeat 3 [--ppm DIR]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+PRECISIONS = {"fp32": 0, "fp64": 1, "mixed": 2}
+SCHEDULES = {"grid": 0, "persistent": 1}
+INTEGRATORS = {"ref": 0, "rk4": 1}
+
+
+def build_scenes(args):
+    from . import scene as S
+    if args.workload == "single":
+        return [S.single_scene(args.width or 640, args.height or 360)]
+    if args.workload == "flythrough":
+        sc = S.flythrough(120, args.width or 1920, args.height or 1080)
+        idx = [round(i * (len(sc) - 1) / max(1, args.frames - 1)) for i in range(args.frames)]
+        return [sc[i] for i in idx]
+    if args.workload == "batched":
+        return S.batched_scenes(args.frames)
+    if args.workload == "photon-ring":
+        return [S.photon_ring_scene(args.width or 4096)]
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def write_ppm(path: str, bgra) -> None:
+    h, w = bgra.shape[:2]
+    with open(path, "wb") as fh:
+        fh.write(f"P6\n{w} {h}\n255\n".encode())
+        fh.write(bgra[..., 2::-1].tobytes())
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--workload", default="flythrough", choices=["single", "flythrough", "batched", "photon-ring"])
+    ap.add_argument("--frames", type=int, default=8)
+    ap.add_argument("--width", type=int, default=0)
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--integrator", default="rk4", choices=list(INTEGRATORS))
+    ap.add_argument("--precision", default="fp32", choices=list(PRECISIONS))
+    ap.add_argument("--schedule", default="grid", choices=list(SCHEDULES))
+    ap.add_argument("--step", type=float, default=0.01)
+    ap.add_argument("--max-steps", type=int, default=4000)
+    ap.add_argument("--band", type=float, default=-1)
+    ap.add_argument("--setup-band", type=float, default=-1)
+    ap.add_argument("--slice", type=int, default=0)
+    ap.add_argument("--refill", type=int, default=0)
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--ppm", default="")
+    args = ap.parse_args(argv)
+
+    import ctypes as C
+
+    import numpy as np
+
+    from . import build, capi
+    from .render import Renderer
+    build.build()
+    scenes = build_scenes(args)
+    opts = capi.default_options(integrator=INTEGRATORS[args.integrator], precision=PRECISIONS[args.precision],
+                                schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
+                                band=args.band, setup_band=args.setup_band, slice_steps=args.slice,
+                                refill_threshold=args.refill)
+    with Renderer(0) as r:
+        cs = r.c_scenes(scenes)
+        import torch
+        bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
+                for s in scenes]
+        frames = (capi.Frame * len(scenes))()
+        for i, b in enumerate(bufs):
+            frames[i].pixels = b.data_ptr()
+        times = []
+        for _ in range(args.repeat):
+            r.render_device(cs, frames, opts)
+            st = r.stats()
+            times.append(st.kernel_ms)
+        rays = sum(s.camera.width() * s.camera.height() for s in scenes)
+        best = min(times)
+        out = {"workload": args.workload, "frames": len(scenes), "rays": rays, "kernel_ms": times,
+               "mrays_per_s": rays / (best * 1e-3) / 1e6, "steps": int(st.steps), "band_rays": int(st.band_rays),
+               "band_steps": int(st.band_steps),
+               "fp32_tflops": st.steps * capi.RK4_FLOPS_PER_STEP / (best * 1e-3) / 1e12}
+        if args.ppm:
+            os.makedirs(args.ppm, exist_ok=True)
+            for i, b in enumerate(bufs):
+                write_ppm(os.path.join(args.ppm, f"frame_{i:04d}.ppm"), b.cpu().numpy())
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

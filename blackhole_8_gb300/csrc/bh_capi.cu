@@ -151,6 +151,9 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
   if (out->block_y == 0) out->block_y = d.block_y;
   if (out->threads_per_block == 0) out->threads_per_block = d.threads_per_block;
   if (out->refill_threshold == 0) out->refill_threshold = d.refill_threshold;
+  if (out->band_step == 0) out->band_step = d.band_step;
+  if (out->setup_band < 0) out->setup_band = d.setup_band;
+  if (out->slice_steps == 0) out->slice_steps = d.slice_steps;
 }
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
@@ -166,16 +169,23 @@ int validate_options(bh_ctx* ctx, const bh_render_options& o) {
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown format %d", o.format);
   if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown schedule %d", o.schedule);
-  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.integrator != BH_INTEGRATOR_RK4)
-    return set_err(ctx, BH_ERR_UNSUPPORTED, "the persistent schedule runs the RK4 integrator only");
+  if (o.schedule == BH_SCHEDULE_PERSISTENT &&
+      (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "the persistent schedule runs RK4 in FP32 or MIXED precision");
   if (!(o.step > 0 && o.step <= 1.0)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "step must be in (0, 1]");
   if (o.max_steps < 1 || o.max_steps > 100000000)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e8]");
   if (!(o.r_escape > 2.0) || !std::isfinite(o.r_escape))
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "r_escape must exceed the horizon (2 M)");
   if (!(o.band >= 0) || !std::isfinite(o.band)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band must be >= 0");
-  if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 1024 || (o.block_x * o.block_y) % 32 != 0)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 1024");
+  if (!(o.band_step > 0 && o.band_step <= 1.0))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_step must be in (0, 1]");
+  if (!(o.setup_band >= 0) || !std::isfinite(o.setup_band))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "setup_band must be >= 0");
+  if (o.slice_steps < 4 || o.slice_steps > 4096)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
+  if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
   if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "threads_per_block must be a multiple of 32 in [32, 256]");
   if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64)
@@ -348,7 +358,17 @@ LaunchParams base_params(const bh_render_options& o) {
   p.step = o.step;
   p.u_escape = 1.0 / o.r_escape;
   p.band = o.band;
+  p.band_step = o.band_step;
+  p.setup_band = o.setup_band;
+  {
+    const double bc = 3.0 * std::sqrt(3.0);
+    const double lo = bc + o.band, hi = bc - o.band;
+    p.eps_band_lo = 1.0 / (lo * lo) - 1.0 / 27.0;
+    p.eps_band_hi = hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300;
+    if (o.band == 0) p.eps_band_lo = p.eps_band_hi = 0.0;  // empty band
+  }
   p.refill_threshold = o.refill_threshold;
+  p.slice_steps = o.slice_steps;
   return p;
 }
 
@@ -441,7 +461,10 @@ void bh_default_options(bh_render_options* o) {
   o->max_steps = 4000;
   o->step = 0.01;
   o->r_escape = 100.0;
-  o->band = 0.01;
+  o->band = 2e-3;
+  o->band_step = 0.01;
+  o->setup_band = 0.25;
+  o->slice_steps = 32;
   o->block_x = 32;
   o->block_y = 4;
   o->threads_per_block = 256;

@@ -84,12 +84,17 @@ struct LaunchParams {
   int32_t max_steps;
   double step;
   double u_escape;            // M / r_escape
-  double band;                // |b - b_c| / M below which MIXED goes FP64
+  double band;                // |b - b_c| / M below which MIXED traces in FP64
+  double band_step;           // RK4 step of the FP64 band
+  double setup_band;          // |b - b_c| / M below which MIXED sets up in FP64
+  double eps_band_lo;         // the FP64 band in terms of eps = 1/(b/M)^2 - 1/27:
+  double eps_band_hi;         //   eps(b_c + band) < eps < eps(b_c - band)
   int64_t total_rays;         // persistent: sum of padded scene ray counts
   DevCounters* counters;
   uint32_t* band_list;        // persistent MIXED: deferred band rays
   uint32_t band_capacity;
   int32_t refill_threshold;
+  int32_t slice_steps;
 };
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.

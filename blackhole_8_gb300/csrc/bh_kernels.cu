@@ -5,15 +5,36 @@
 // plane through the hole (:170-193; the basis is orthonormal, so the
 // reference's 3x3 inverse is a transpose here), (3) integrates the photon
 // orbit with either the reference's 20+20-step trapezoid rule in u with chord
-// collisions (:202-296) or RK4 in phi on u'' = -u + 3 u^2 (u in units of 1/M)
+// collisions (:202-296) or classical RK4 in phi on u'' = -u + 3 u^2 (u = M/r)
 // with horizon, escape and disc-plane events, (4) samples the disc or
 // background texture and (5) stores the pixel.
 //
-// The RK4 path is FMA- and divergence-bound; it has no dense contraction, so
-// there is no tensor-core work. Textures (a few MB) stay in L2 and are read
-// through the read-only path once per ray.
+// RK4 details. The state is x = u - 1/3, w = du/dphi: the orbit equation
+// becomes x'' = x + 3 x^2 (no constant term), so FP32 keeps relative
+// precision near the unstable photon orbit x = 0. The change of variables is
+// affine, so the RK4 trajectory is the same as in u. Because the right-hand
+// side does not depend on w, the classical RK4 step is written in its
+// Runge-Kutta-Nystrom form (same method, 18 FP32 instructions, 28 flops).
+// Horizon and escape are tested once per block of 4 steps; a block that
+// overshoots is rolled back and replayed one step at a time.
+//
+// Mixed precision. FP32 rays keep the first integral
+// eps = w^2 - x^2 - 2 x^3 (= 1/b^2 - 1/27, the G of blackhole_solution.h:
+// 27-29) only to FP32 rounding, and near x = 0 (the saddle of the photon
+// orbit) that drift is amplified by 1/|b - b_c|. The mixed tracer therefore
+// (a) takes b, eps and the plane basis from FP64 ray setup for rays with
+// |b - b_c| < setup_band, (b) projects (x, w) back onto eps = const after
+// every 4-step block spent near the saddle (|x| < 0.1), (c) traces rays with
+// |b - b_c| < band fully in FP64 with the band step, and (d) refines
+// disc-plane crossings in FP64.
+//
+// The path has no dense contraction, so there is no tensor-core work; it is
+// bound by FP32 issue. Textures (a few MB) stay in L2 and are read once per
+// ray through the read-only path.
 #include <math_constants.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 #include "bh_internal.h"
 
@@ -49,6 +70,8 @@ __device__ __forceinline__ V3<R> normalize(V3<R> a) {
   const R k = l != R(0) ? R(1) / l : R(0);
   return a * k;
 }
+template <typename R, typename S>
+__device__ __forceinline__ V3<R> cast3(V3<S> a) { return {R(a.x), R(a.y), R(a.z)}; }
 
 // Precision-dependent view of a DevScene field.
 template <typename R>
@@ -316,101 +339,190 @@ __device__ Hit trace_ref(const DevScene& s, int x, int y) {
 }
 
 // ---------------------------------------------------------------------------
-// RK4 in phi on u'' = -u + 3 u^2 (u = M / r), state (u, w = du/dphi).
+// RK4 in phi on x'' = x + 3 x^2, x = M/r - 1/3.
 template <typename R>
 struct Rk4Consts {
-  R h, hh, h6;
-  R u_esc;
+  R h, hh, q, q2, h26, h6;  // h, h/2, h^2/4, h^2/2, h^2/6, h/6
+  R x_esc, x_hor;           // escape: x <= M/r_esc - 1/3; horizon: x >= 1/2 - 1/3
   int kmax;
 };
 
-// One RK4 step: 22 FP32 instructions, 36 flops (FMA = 2).
 template <typename R>
-__device__ __forceinline__ void rk4_step(R& u, R& w, R h, R hh, R h6) {
-  const R a1 = fma(R(3) * u, u, -u);
-  const R u2 = fma(hh, w, u), w2 = fma(hh, a1, w);
-  const R a2 = fma(R(3) * u2, u2, -u2);
-  const R u3 = fma(hh, w2, u), w3 = fma(hh, a2, w);
-  const R a3 = fma(R(3) * u3, u3, -u3);
-  const R u4 = fma(h, w3, u), w4 = fma(h, a3, w);
-  const R a4 = fma(R(3) * u4, u4, -u4);
-  u = fma(h6, (fma(R(2), w2 + w3, w) + w4), u);
-  w = fma(h6, (fma(R(2), a2 + a3, a1) + a4), w);
+__device__ __forceinline__ Rk4Consts<R> rk4_consts(double h, double u_escape, int kmax) {
+  Rk4Consts<R> c;
+  c.h = R(h);
+  c.hh = R(h * 0.5);
+  c.q = R(h * h * 0.25);
+  c.q2 = R(h * h * 0.5);
+  c.h26 = R(h * h / 6.0);
+  c.h6 = R(h / 6.0);
+  c.x_esc = R(u_escape - 1.0 / 3.0);
+  c.x_hor = R(0.5 - 1.0 / 3.0);
+  c.kmax = kmax;
+  return c;
 }
+
+template <typename R>
+__device__ __forceinline__ R fx(R x) { return x * fma(R(3), x, R(1)); }
+
+// One classical RK4 step in Runge-Kutta-Nystrom form:
+// 18 FP32 instructions, 28 flops (FMA = 2).
+template <typename R>
+__device__ __forceinline__ void rk4_step(R& x, R& w, const Rk4Consts<R>& c) {
+  const R k1 = fx(x);
+  const R s1 = fma(c.hh, w, x);
+  const R k2 = fx(s1);
+  const R s2 = fma(c.q, k1, s1);
+  const R k3 = fx(s2);
+  const R s3a = fma(c.h, w, x);
+  const R s3 = fma(c.q2, k2, s3a);
+  const R k4 = fx(s3);
+  const R A = k2 + k3;
+  const R S = A + k1;
+  x = fma(c.h26, S, s3a);
+  w = fma(c.h6, (S + A) + k4, w);
+}
+
+template <typename R>
+__device__ __forceinline__ void rk4_partial(R& x, R& w, R h) {
+  Rk4Consts<R> c;
+  c.h = h;
+  c.hh = h * R(0.5);
+  c.q = h * h * R(0.25);
+  c.q2 = h * h * R(0.5);
+  c.h26 = h * h * R(1.0 / 6.0);
+  c.h6 = h * R(1.0 / 6.0);
+  rk4_step<R>(x, w, c);
+}
+
+// Moves (x, w) back onto w^2 - x^2 - 2 x^3 = eps along the gradient.
+__device__ __forceinline__ void project_energy(float& x, float& w, float eps) {
+  const float g = x * x * fmaf(2.f, x, 1.f);
+  const float r = fmaf(w, w, -g) - eps;
+  const float gx = -2.f * x * fmaf(3.f, x, 1.f);
+  const float gw = 2.f * w;
+  const float g2 = fmaf(gx, gx, gw * gw);
+  if (g2 > 1e-30f) {
+    const float k = __fdividef(r, g2);
+    x = fmaf(-k, gx, x);
+    w = fmaf(-k, gw, w);
+  }
+}
+__device__ __forceinline__ void project_energy(double&, double&, double) {}
 
 enum : int { kRunning = 0, kHorizon = 1, kEscape = 2, kDisc = 3, kMaxSteps = 4, kDone = 5 };
 
 template <typename R>
 struct RayState {
-  R u, w;       // current state
-  R ua, wa;     // state before the last step (escape refinement)
+  R x, w;       // current state
+  R xa, wa;     // state before the last step (escape refinement)
+  R eps;        // first integral w^2 - x^2 - 2x^3 = 1/b^2 - 1/27 (units of M)
   R phi0;       // initial in-plane angle of the camera
   R dcr;        // offset of the next disc-plane crossing from phi0
-  R ev;         // event payload: disc crossing u
+  R ev;         // event payload: u at the disc crossing
   int k, kc;    // steps taken, step index holding the next crossing
   int status;
   V3<R> yv, xv;
 };
 
-// Sets up the RK4 state of pixel (x, y). Returns false when the ray needs no
-// integration (it heads into the centre: b < 1e-6 M gives the horizon).
-template <typename R>
-__device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& ray, R h, RayState<R>& st) {
-  const R M = BH_S(R, s, mass);
-  st.yv = ray.yv;
-  st.xv = ray.xv;
+// Sets up the RK4 state from a plane ray computed in precision RS.
+template <typename R, typename RS>
+__device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<RS>& ray, double h, RayState<R>& st) {
+  const RS M = RS(s.mass);
+  st.yv = cast3<R>(ray.yv);
+  st.xv = cast3<R>(ray.xv);
   st.k = 0;
   st.kc = 0x7fffffff;
   st.dcr = R(0);
   st.ev = R(0);
-  const R r0 = sqrt(ray.F0 * ray.F0 + ray.F1 * ray.F1 + ray.b * ray.b);
-  const R bm = ray.b / M;
-  st.u = M / r0;
-  st.phi0 = atan2(ray.b, ray.F1);
-  if (!(bm > R(1e-6))) {
+  const RS r0 = sqrt(ray.F0 * ray.F0 + ray.F1 * ray.F1 + ray.b * ray.b);
+  const RS bm = ray.b / M;
+  const RS x0 = M / r0 - RS(1.0 / 3.0);
+  const RS phi0 = atan2(ray.b, ray.F1);
+  st.x = R(x0);
+  st.phi0 = R(phi0);
+  if (!(bm > RS(1e-6))) {  // heads into the centre
     st.status = kHorizon;
     st.w = R(0);
+    st.eps = R(0);
     return;
   }
-  const R g0 = R(1) / (bm * bm) - st.u * st.u * (R(1) - R(2) * st.u);
-  st.w = copysign(sqrt(fmax(g0, R(0))), ray.F1);
+  const RS eps = RS(1) / (bm * bm) - RS(1.0 / 27.0);
+  st.eps = R(eps);
+  st.w = R(copysign(sqrt(fmax(eps + x0 * x0 * fma(RS(2), x0, RS(1)), RS(0))), ray.F1));
   st.status = kRunning;
   if (s.disc_on) {
-    const V3<R> n = BH_V(R, s, dn);
-    const R A = dot(n, ray.yv), B = dot(n, ray.xv);
-    if (A * A + B * B > R(1e-24)) {
-      R d = fmod(atan2(B, A) + kPi<R>() * R(0.5) - st.phi0, kPi<R>());
-      if (d <= R(0)) d += kPi<R>();
-      st.dcr = d;
-      st.kc = (int)floor(d / h);
+    const V3<RS> n = BH_V(RS, s, dn);
+    const RS A = dot(n, ray.yv), B = dot(n, ray.xv);
+    if (A * A + B * B > RS(1e-24)) {
+      RS d = fmod(atan2(B, A) + kPi<RS>() * RS(0.5) - phi0, kPi<RS>());
+      if (d <= RS(0)) d += kPi<RS>();
+      st.dcr = R(d);
+      st.kc = (int)floor(d / RS(h));
     }
   }
 }
 
-// Disc-plane crossing inside step kc: a partial RK4 step of length
-// dcr - kc*h from the state at the step start, in precision RC.
-template <typename R, typename RC>
-__device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R h) {
+// u at a disc-plane crossing: a partial RK4 step of length dcr - kc*h from
+// the state at the start of step kc, in precision RC.
+template <typename RC, typename R>
+__device__ __forceinline__ RC crossing_u(const RayState<R>& st, R h) {
   const RC sc = RC(st.dcr) - RC(st.kc) * RC(h);
-  RC u = RC(st.u), w = RC(st.w);
-  rk4_step<RC>(u, w, sc, sc * RC(0.5), sc * RC(1.0 / 6.0));
-  const RC M = RC(s.mass);
-  if (u < RC(0.5)) {
-    const RC rc = RC(1) / u;
-    if (rc * M >= RC(s.r_in) && rc * M <= RC(s.r_out)) {
-      st.ev = R(u);
-      return true;
+  RC x = RC(st.x), w = RC(st.w);
+  rk4_partial<RC>(x, w, sc);
+  return x + RC(1.0 / 3.0);
+}
+
+template <typename RC>
+__device__ __forceinline__ bool on_disc(const DevScene& s, RC u) {
+  if (!(u < RC(0.5))) return false;
+  const RC rc = BH_S(RC, s, mass) / u;
+  return rc >= BH_S(RC, s, r_in) && rc <= BH_S(RC, s, r_out);
+}
+
+// FP64 root refinement of an FP32 crossing whose radius lies within 2e-3 M of
+// a disc edge (out of line).
+__device__ __noinline__ float crossing_u_fp64(const RayState<float>& st, float h, int* hit,
+                                              const DevScene& s) {
+  const double u = crossing_u<double>(st, h);
+  *hit = on_disc<double>(s, u);
+  return float(u);
+}
+
+// Disc-plane crossing inside step kc. kRefine64: FP32 crossing with FP64
+// refinement near the disc edges (mixed tracer).
+template <typename R, bool kRefine64>
+__device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R h) {
+  R u = crossing_u<R>(st, h);
+  bool hit = on_disc<R>(s, u);
+  if (kRefine64) {
+    const R rc = BH_S(R, s, mass) / u;
+    const R tol = R(2e-3) * BH_S(R, s, mass);
+    if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
+      int h64 = 0;
+      u = R(crossing_u_fp64(reinterpret_cast<const RayState<float>&>(st), float(h), &h64, s));
+      hit = h64 != 0;
     }
+  }
+  if (hit) {
+    st.ev = u;
+    return true;
   }
   st.dcr += kPi<R>();
   st.kc = (int)floor(st.dcr / h);
   return false;
 }
 
-// Advances up to `budget` steps; returns the steps taken.
-template <typename R, typename RC>
+template <typename R>
+__device__ __forceinline__ bool inside(R x, const Rk4Consts<R>& c) { return x > c.x_esc && x < c.x_hor; }
+
+// Advances up to `budget` steps; returns the steps taken. kMixed (FP32 mixed
+// tracer): energy projection near the saddle and FP64 refinement of
+// crossings near the disc edges.
+template <typename R, bool kMixed>
 __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, const Rk4Consts<R>& c,
                                            int budget) {
+  constexpr bool kProject = kMixed;
   int taken = 0;
   while (st.status == kRunning) {
     if (st.k >= c.kmax) {
@@ -418,32 +530,50 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
       break;
     }
     if (st.k == st.kc) {
-      if (cross_disc<R, RC>(s, st, c.h)) {
+      if (cross_disc<R, kMixed>(s, st, c.h)) {
         st.status = kDisc;
         break;
       }
     }
     if (taken >= budget) break;
     const int kstop = min(min(st.kc, c.kmax), st.k + (budget - taken));
-    R u = st.u, w = st.w, ua = u, wa = w;
+    R x = st.x, w = st.w;
     int k = st.k;
+    // blocks of 4 steps, event test once per block
+    while (k + 4 <= kstop) {
+      const R x0 = x, w0 = w;
+      rk4_step<R>(x, w, c);
+      rk4_step<R>(x, w, c);
+      rk4_step<R>(x, w, c);
+      rk4_step<R>(x, w, c);
+      if (!inside(x, c)) {
+        x = x0;
+        w = w0;
+        break;
+      }
+      k += 4;
+      if (kProject) {
+        if (fabs(x) < R(0.1)) project_energy(x, w, st.eps);
+      }
+    }
+    // single steps up to kstop or the event
+    R xa = x, wa = w;
     int ev = kRunning;
-#pragma unroll 2
-    for (; k < kstop;) {
-      ua = u;
+    while (k < kstop) {
+      xa = x;
       wa = w;
-      rk4_step<R>(u, w, c.h, c.hh, c.h6);
+      rk4_step<R>(x, w, c);
       ++k;
-      if (!(u < R(0.5)) || u <= c.u_esc) {
-        ev = (u <= c.u_esc) ? kEscape : kHorizon;
+      if (!inside(x, c)) {
+        ev = x <= c.x_esc ? kEscape : kHorizon;
         break;
       }
     }
     taken += k - st.k;
     st.k = k;
-    st.u = u;
+    st.x = x;
     st.w = w;
-    st.ua = ua;
+    st.xa = xa;
     st.wa = wa;
     st.status = ev;
   }
@@ -452,7 +582,7 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
 
 // Shades a finished RK4 ray.
 template <typename R>
-__device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c) {
+__device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c, double u_escape) {
   Hit hit = {make_uchar4(0, 0, 0, 255), BH_CLASS_HORIZON, 0.f};
   if (st.status == kMaxSteps) {
     hit.cls = BH_CLASS_MAXSTEPS;
@@ -464,25 +594,25 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     hit.aux = float(R(1) / st.ev);
     hit.bgra = disc_color(s, p);
   } else if (st.status == kEscape) {
-    // Cubic Hermite through (ua, wa) and (u, w) over the last step; Newton
-    // for the parameter t where u(t) = u_esc.
-    const R ua = st.ua, ub = st.u, ha = c.h * st.wa, hb = c.h * st.w, ue = c.u_esc;
-    R t = (ua - ue) / (ua - ub);
+    // Cubic Hermite through (xa, wa) and (x, w) over the last step; Newton
+    // for the parameter t where x(t) = x_esc.
+    const R xa = st.xa, xb = st.x, ha = c.h * st.wa, hb = c.h * st.w, xe = c.x_esc;
+    R t = (xa - xe) / (xa - xb);
     t = fmin(fmax(t, R(0)), R(1));
     for (int i = 0; i < 3; ++i) {
       const R t2 = t * t, t3 = t2 * t;
-      const R p = (R(2) * t3 - R(3) * t2 + R(1)) * ua + (t3 - R(2) * t2 + t) * ha +
-                  (R(3) * t2 - R(2) * t3) * ub + (t3 - t2) * hb;
-      const R dp = (R(6) * t2 - R(6) * t) * ua + (R(3) * t2 - R(4) * t + R(1)) * ha +
-                   (R(6) * t - R(6) * t2) * ub + (R(3) * t2 - R(2) * t) * hb;
-      t = fmin(fmax(t - (p - ue) / dp, R(0)), R(1));
+      const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha +
+                  (R(3) * t2 - R(2) * t3) * xb + (t3 - t2) * hb;
+      const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
+                   (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
+      t = fmin(fmax(t - (p - xe) / dp, R(0)), R(1));
     }
     const R t2 = t * t;
-    const R dp = (R(6) * t2 - R(6) * t) * ua + (R(3) * t2 - R(4) * t + R(1)) * ha +
-                 (R(6) * t - R(6) * t2) * ub + (R(3) * t2 - R(2) * t) * hb;
+    const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
+                 (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
     const R we = dp / c.h;
     const R phie = st.phi0 + (R(st.k - 1) + t) * c.h;
-    const R psi = phie + atan2(ue, -we);
+    const R psi = phie + atan2(R(u_escape), -we);
     hit.cls = BH_CLASS_MISS;
     hit.aux = float(psi - kPi<R>());
     if (s.has_bg) {
@@ -493,29 +623,54 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
   return hit;
 }
 
-template <typename R>
-__device__ __forceinline__ Rk4Consts<R> rk4_consts(const LaunchParams& p) {
-  Rk4Consts<R> c;
-  c.h = R(p.step);
-  c.hh = R(p.step * 0.5);
-  c.h6 = R(p.step / 6.0);
-  c.u_esc = R(p.u_escape);
-  c.kmax = p.max_steps;
-  return c;
-}
+// ---------------------------------------------------------------------------
+// per-ray drivers
+constexpr double kBC = 5.196152422706632;  // 3 sqrt(3)
 
-// Full RK4 trace of one pixel in precision R (crossing refinement in RC).
-template <typename R, typename RC>
-__device__ Hit trace_rk4(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
-  const Rk4Consts<R> c = rk4_consts<R>(p);
+// Full trace in one precision R.
+template <typename R, bool kMixed>
+__device__ Hit trace_rk4(const DevScene& s, int x, int y, double h, double u_escape, int kmax, int* steps) {
+  const Rk4Consts<R> c = rk4_consts<R>(h, u_escape, kmax);
   RayState<R> st;
-  init_rk4<R>(s, make_ray<R>(s, x, y), c.h, st);
-  *steps = advance_rk4<R, RC>(s, st, c, 0x7fffffff);
-  return finish_rk4<R>(s, st, c);
+  init_rk4<R, R>(s, make_ray<R>(s, x, y), h, st);
+  *steps = advance_rk4<R, kMixed>(s, st, c, 0x7fffffff);
+  return finish_rk4<R>(s, st, c, u_escape);
 }
 
-__device__ __forceinline__ bool in_band(const DevScene& s, float b, double band) {
-  return fabsf(b / s.mass_f - 5.19615242270663188f) < float(band);
+// FP64 trace of a band ray (out of line: keeps FP64 register pressure away
+// from the FP32 callers).
+__device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
+  return trace_rk4<double, false>(s, x, y, p.band_step, p.u_escape, p.max_steps, steps);
+}
+
+// First integral eps = 1/(b/M)^2 - 1/27 of pixel (x, y) in FP64:
+// b = |F x e| / |e| with e = F - pv, so (b/M)^-2 = |e|^2 M^2 / |F x e|^2
+// (about 25 FP64 operations, no square root).
+__device__ __noinline__ double eps_fp64(const DevScene& s, int x, int y) {
+  const V3<double> F = {s.F[0], s.F[1], s.F[2]};
+  const double a = s.half_w - double(x), c = s.half_h - double(y);
+  const V3<double> e = V3<double>{s.E0[0], s.E0[1], s.E0[2]} + V3<double>{s.vy[0], s.vy[1], s.vy[2]} * a +
+                       V3<double>{s.vz[0], s.vz[1], s.vz[2]} * c;
+  const V3<double> fe = cross(F, e);
+  return dot(e, e) * (s.mass * s.mass) / dot(fe, fe) - 1.0 / 27.0;
+}
+
+// Sets up one ray of the mixed tracer. Returns false when the ray belongs to
+// the FP64 band (nothing is traced then). Rays within setup_band of b_c take
+// their first integral from FP64; everything else of the setup is FP32.
+__device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, const LaunchParams& p,
+                                            RayState<float>& st) {
+  const PlaneRay<float> r = make_ray<float>(s, x, y);
+  init_rk4<float, float>(s, r, p.step, st);
+  if (fabsf(r.b / s.mass_f - float(kBC)) < float(p.setup_band)) {
+    const double eps = eps_fp64(s, x, y);
+    if (eps > p.eps_band_lo && eps < p.eps_band_hi) return false;
+    if (st.status == kRunning) {
+      st.eps = float(eps);
+      st.w = copysignf(sqrtf(fmaxf(st.eps + st.x * st.x * fmaf(2.f, st.x, 1.f), 0.f)), st.w);
+    }
+  }
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -524,20 +679,11 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
   const unsigned m = __activemask();
   unsigned lo = (unsigned)min(v, 0xffffffffull);
   lo = __reduce_add_sync(m, lo);
-  if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(dst, (unsigned long long)lo);
-}
-
-// FP64 trace of a band ray that did not fit the deferral list; kept out of
-// line so the FP32 kernel's register allocation does not carry it.
-__device__ __noinline__ int trace_band_inline(const DevScene& s, int x, int y, const LaunchParams& p) {
-  int steps = 0;
-  const Hit h = trace_rk4<double, double>(s, x, y, p, &steps);
-  store_hit(s, p.format, x, y, h);
-  return steps;
+  if ((threadIdx.x & 31) == __ffs(m) - 1 && lo) atomicAdd(dst, (unsigned long long)lo);
 }
 
 // GRID schedule: one thread per pixel, gridDim.z = scene.
-__global__ void grid_kernel(LaunchParams p) {
+__global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   const DevScene& s = p.scenes[blockIdx.z];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -548,17 +694,19 @@ __global__ void grid_kernel(LaunchParams p) {
   if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
     h = p.precision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
   } else if (p.precision == BH_PRECISION_FP64) {
-    h = trace_rk4<double, double>(s, x, y, p, &steps);
+    h = trace_rk4<double, false>(s, x, y, p.step, p.u_escape, p.max_steps, &steps);
   } else if (p.precision == BH_PRECISION_MIXED) {
-    const PlaneRay<float> r32 = make_ray<float>(s, x, y);
-    if (in_band(s, r32.b, p.band)) {
-      band_ray = 1;
-      h = trace_rk4<double, double>(s, x, y, p, &steps);
+    RayState<float> st;
+    if (setup_mixed(s, x, y, p, st)) {
+      const Rk4Consts<float> c = rk4_consts<float>(p.step, p.u_escape, p.max_steps);
+      steps = advance_rk4<float, true>(s, st, c, 0x7fffffff);
+      h = finish_rk4<float>(s, st, c, p.u_escape);
     } else {
-      h = trace_rk4<float, double>(s, x, y, p, &steps);
+      band_ray = 1;
+      h = trace_band(s, x, y, p, &steps);
     }
   } else {
-    h = trace_rk4<float, float>(s, x, y, p, &steps);
+    h = trace_rk4<float, false>(s, x, y, p.step, p.u_escape, p.max_steps, &steps);
   }
   store_hit(s, p.format, x, y, h);
   if (p.counters) {
@@ -574,106 +722,140 @@ __global__ void grid_kernel(LaunchParams p) {
 // ---------------------------------------------------------------------------
 // PERSISTENT schedule.
 //
-// Ray index space: scenes back to back, each padded to 8x4 pixel tiles, 32
-// consecutive indices per tile. Every warp owns 32 lanes = 32 rays in flight;
-// after each slice of integration steps it counts its idle lanes (ballot)
-// and, once at least `refill_threshold` are idle, takes that many new ray
-// indices from the global queue with one atomicAdd and hands them out by
-// lane rank. With MIXED precision, rays inside the FP64 band are not traced
-// here: their indices go to the band list and the FP64 pass takes them.
+// Work is a queue of 32-ray items: 8x4-pixel tiles over all scenes of the call
+// (scenes back to back, each padded to whole tiles), or 32 entries of the
+// band list in the FP64 pass. Each warp keeps one pending item: a 32-bit mask
+// of its rays not yet handed to a lane. After each slice of integration steps
+// the warp counts its idle lanes (ballot); once at least `refill_threshold`
+// are idle it hands them the pending item's next rays in lane order
+// (re-packing the warp), and takes the next item from the queue (one
+// atomicAdd per 32 rays) when the pending one runs dry. A tile's scene is
+// looked up once per tile. With MIXED precision, rays of the FP64 band are
+// not traced in the FP32 pass: their indices go to the band list, which a
+// second persistent pass traces in FP64.
 
-__device__ __forceinline__ int find_scene(const LaunchParams& p, long long g) {
+__device__ __forceinline__ int find_scene(const LaunchParams& p, long long ray) {
   int lo = 0, hi = p.n_scenes - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (p.scenes[mid].ray_begin <= g) lo = mid;
+    if (p.scenes[mid].ray_begin <= ray) lo = mid;
     else hi = mid - 1;
   }
   return lo;
 }
 
+// Pixel of ray `local` (index within its scene).
 __device__ __forceinline__ bool ray_pixel(const DevScene& s, long long local, int* x, int* y) {
   const long long tile = local >> 5;
   const int l = (int)(local & 31);
-  *x = (int)(tile % s.tiles_x) * 8 + (l & 7);
-  *y = (int)(tile / s.tiles_x) * 4 + (l >> 3);
+  const int ty = (int)(tile / s.tiles_x);
+  const int tx = (int)(tile - (long long)ty * s.tiles_x);
+  *x = tx * 8 + (l & 7);
+  *y = ty * 4 + (l >> 3);
   return *x < s.width && *y < s.height;
 }
 
-constexpr int kSlice = 16;  // integration steps between refill checks
+// Sets up the FP32-pass ray `item` (global ray index) on this lane; returns
+// false when the lane stays idle (padding pixel or deferred band ray).
+template <bool kMixed>
+__device__ __forceinline__ bool take_fp32_ray(const LaunchParams& p, int scene, long long item,
+                                              RayState<float>& st, int* px, int* py, unsigned long long* steps) {
+  const DevScene& s = p.scenes[scene];
+  if (!ray_pixel(s, item - s.ray_begin, px, py)) return false;
+  if (!kMixed) {
+    init_rk4<float, float>(s, make_ray<float>(s, *px, *py), p.step, st);
+    return true;
+  }
+  if (setup_mixed(s, *px, *py, p, st)) return true;
+  const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
+  if (slot < p.band_capacity) {
+    p.band_list[slot] = (uint32_t)item;
+  } else {  // list full: trace inline in FP64
+    atomicAdd(&p.counters->band_overflow, 1ull);
+    int bsteps = 0;
+    const Hit hb = trace_band(s, *px, *py, p, &bsteps);
+    store_hit(s, p.format, *px, *py, hb);
+    atomicAdd(&p.counters->band_rays, 1ull);
+    atomicAdd(&p.counters->band_steps, (unsigned long long)bsteps);
+    atomicAdd(&p.counters->rays, 1ull);
+    *steps += bsteps;
+  }
+  return false;
+}
 
-template <typename R, typename RC, bool kBandPass>
+// kPass: 0 = FP32 plain, 1 = FP32 mixed (band rays deferred), 2 = FP64 band.
+template <int kPass>
 __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
+  using R = typename std::conditional<kPass == 2, double, float>::type;
   const int lane = threadIdx.x & 31;
-  const Rk4Consts<R> c = rk4_consts<R>(p);
-  const long long total = kBandPass ? 0 : p.total_rays;
+  const unsigned lt_mask = (1u << lane) - 1;
+  const double h = kPass == 2 ? p.band_step : p.step;
+  const Rk4Consts<R> c = rk4_consts<R>(h, p.u_escape, p.max_steps);
+  const long long n_items =
+      kPass == 2 ? (long long)min(*(volatile unsigned long long*)&p.counters->band_count,
+                                  (unsigned long long)p.band_capacity)
+                 : p.total_rays;
+  unsigned long long* queue = kPass == 2 ? &p.counters->band_next : &p.counters->next_ray;
   RayState<R> st;
   st.status = kDone;
   int scene = 0, px = 0, py = 0;
-  bool exhausted = false;
   unsigned long long steps = 0, rays = 0;
   const int thr = max(1, min(32, p.refill_threshold));
+  long long pend_base = 0;  // first item index of the pending 32
+  unsigned pend_mask = 0;   // its items not yet handed out
+  int pend_scene = 0;
+  bool exhausted = false;
 
   for (;;) {
-    const unsigned idle = __ballot_sync(kFull, st.status == kDone);
-    if (idle == kFull && exhausted) break;
-    if (!exhausted && (__popc(idle) >= thr || idle == kFull)) {
-      const int n = __popc(idle);
-      unsigned long long base = 0;
-      if (lane == 0) {
-        base = atomicAdd(kBandPass ? &p.counters->band_next : &p.counters->next_ray,
-                         (unsigned long long)n);
-      }
-      base = __shfl_sync(kFull, base, 0);
-      const unsigned long long limit =
-          kBandPass ? min((unsigned long long)*(volatile unsigned long long*)&p.counters->band_count,
-                          (unsigned long long)p.band_capacity)
-                    : (unsigned long long)total;
-      if (base + n >= limit) exhausted = true;
-      if (st.status == kDone) {
-        const unsigned long long g = base + __popc(idle & ((1u << lane) - 1));
-        if (g < limit) {
-          const long long ray = kBandPass ? (long long)p.band_list[g] : (long long)g;
-          scene = find_scene(p, ray);
-          const DevScene& s = p.scenes[scene];
-          if (ray_pixel(s, ray - s.ray_begin, &px, &py)) {
-            ++rays;
-            if (kBandPass) {
-              init_rk4<R>(s, make_ray<R>(s, px, py), c.h, st);
-            } else {
-              const PlaneRay<R> r = make_ray<R>(s, px, py);
-              bool defer = false;
-              if (p.precision == BH_PRECISION_MIXED && in_band(s, float(r.b), p.band)) {
-                const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
-                if (slot < p.band_capacity) {
-                  p.band_list[slot] = (uint32_t)ray;
-                  defer = true;
-                } else {
-                  // list full: trace this band ray inline in FP64
-                  atomicAdd(&p.counters->band_overflow, 1ull);
-                  const int bsteps = trace_band_inline(s, px, py, p);
-                  atomicAdd(&p.counters->band_rays, 1ull);
-                  atomicAdd(&p.counters->band_steps, (unsigned long long)bsteps);
-                  steps += bsteps;
-                  defer = true;
-                }
-              }
-              if (defer) {
-                --rays;
-                st.status = kDone;
-              } else {
-                init_rk4<R>(s, r, c.h, st);
-              }
-            }
+    unsigned idle = __ballot_sync(kFull, st.status == kDone);
+    if (idle == kFull && exhausted && pend_mask == 0) break;
+    if (__popc(idle) >= thr || idle == kFull) {
+      // hand out pending items until every lane is busy or work runs out
+      while (idle) {
+        if (pend_mask == 0) {
+          if (exhausted) break;
+          unsigned long long t = 0;
+          if (lane == 0) t = atomicAdd(queue, 32ull);
+          t = __shfl_sync(kFull, t, 0);
+          if ((long long)t >= n_items) {
+            exhausted = true;
+            break;
+          }
+          pend_base = (long long)t;
+          const long long left = n_items - pend_base;
+          pend_mask = left >= 32 ? kFull : ((1u << left) - 1u);
+          if constexpr (kPass != 2) {
+            int sc = 0;
+            if (lane == 0) sc = find_scene(p, pend_base);
+            pend_scene = __shfl_sync(kFull, sc, 0);
           }
         }
+        const int n = min(__popc(idle), __popc(pend_mask));
+        const int rank = __popc(idle & lt_mask);
+        if (((idle >> lane) & 1u) && rank < n) {
+          const long long item = pend_base + (long long)__fns(pend_mask, 0, rank + 1);
+          if constexpr (kPass == 2) {
+            const long long ray = (long long)p.band_list[item];
+            scene = find_scene(p, ray);
+            const DevScene& s = p.scenes[scene];
+            if (ray_pixel(s, ray - s.ray_begin, &px, &py)) {
+              ++rays;
+              init_rk4<R, R>(s, make_ray<R>(s, px, py), h, st);
+            }
+          } else {
+            scene = pend_scene;
+            if (take_fp32_ray<kPass == 1>(p, scene, item, st, &px, &py, &steps)) ++rays;
+          }
+        }
+        for (int i = 0; i < n; ++i) pend_mask &= pend_mask - 1u;  // drop the n lowest items
+        idle = __ballot_sync(kFull, st.status == kDone);
       }
     }
     if (st.status != kDone) {
       const DevScene& s = p.scenes[scene];
-      steps += advance_rk4<R, RC>(s, st, c, kSlice);
+      steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
       if (st.status != kRunning) {
-        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c));
+        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c, p.u_escape));
         st.status = kDone;
       }
     }
@@ -685,12 +867,12 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
     wrays += __shfl_xor_sync(kFull, wrays, o);
   }
   if (lane == 0) {
-    atomicAdd(kBandPass ? &p.counters->band_steps : &p.counters->steps, wsteps);
-    atomicAdd(kBandPass ? &p.counters->band_rays : &p.counters->rays, wrays);
-    if (kBandPass) {
-      atomicAdd(&p.counters->steps, wsteps);
-      atomicAdd(&p.counters->rays, wrays);
+    if (kPass == 2) {
+      atomicAdd(&p.counters->band_steps, wsteps);
+      atomicAdd(&p.counters->band_rays, wrays);
     }
+    atomicAdd(&p.counters->steps, wsteps);
+    atomicAdd(&p.counters->rays, wrays);
   }
 }
 
@@ -742,30 +924,21 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
 }
 
 cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream) {
-  if (p.precision == BH_PRECISION_FP64) {
-    persistent_kernel<double, double, false><<<blocks, threads, 0, stream>>>(p);
-    return cudaGetLastError();
-  }
   if (p.precision == BH_PRECISION_MIXED) {
-    persistent_kernel<float, double, false><<<blocks, threads, 0, stream>>>(p);
+    persistent_kernel<1><<<blocks, threads, 0, stream>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    persistent_kernel<double, double, true><<<blocks, threads, 0, stream>>>(p);
+    persistent_kernel<2><<<blocks, threads, 0, stream>>>(p);
     return cudaGetLastError();
   }
-  persistent_kernel<float, float, false><<<blocks, threads, 0, stream>>>(p);
+  persistent_kernel<0><<<blocks, threads, 0, stream>>>(p);
   return cudaGetLastError();
 }
 
 cudaError_t persistent_occupancy(const LaunchParams& p, int threads, int* blocks_per_sm) {
-  if (p.precision == BH_PRECISION_FP64)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm,
-                                                         persistent_kernel<double, double, false>, threads, 0);
   if (p.precision == BH_PRECISION_MIXED)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm,
-                                                         persistent_kernel<float, double, false>, threads, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_kernel<float, float, false>,
-                                                       threads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_kernel<1>, threads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_kernel<0>, threads, 0);
 }
 
 cudaError_t launch_fp32_probe(float* sink, int blocks, int threads, int iters, cudaStream_t stream) {

@@ -148,15 +148,21 @@ typedef struct bh_render_options {
   int32_t max_steps;         /* RK4 step cap (default 4000) */
   double step;               /* RK4 step in phi (default 0.01) */
   double r_escape;           /* RK4 escape radius in units of M (default 100) */
-  double band;               /* MIXED: FP64 band half-width of |b - 3 sqrt(3) M|
-                                in units of M (default 0.01) */
+  double band;               /* MIXED: rays with |b - 3 sqrt(3) M| < band * M are
+                                traced in FP64 with step band_step (default 2e-3) */
   int32_t block_x;           /* GRID block shape (default 32 x 4) */
   int32_t block_y;
   int32_t threads_per_block; /* PERSISTENT block size (default 256) */
   int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
   int32_t refill_threshold;  /* PERSISTENT: refill a warp once this many lanes
                                 are idle (default 8) */
-  int32_t reserved[9];
+  double band_step;          /* MIXED: RK4 step of the FP64 band (default 0.01) */
+  double setup_band;         /* MIXED: rays with |b - 3 sqrt(3) M| < setup_band * M
+                                get their impact parameter, conserved energy and
+                                plane basis from FP64 ray setup (default 0.25) */
+  int32_t slice_steps;       /* PERSISTENT: integration steps between refill
+                                checks (default 32) */
+  int32_t reserved[5];
 } bh_render_options;
 
 /* Counters of the most recent render on a context. */
