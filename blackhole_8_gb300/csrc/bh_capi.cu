@@ -154,6 +154,7 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
   if (out->band_step == 0) out->band_step = d.band_step;
   if (out->setup_band < 0) out->setup_band = d.setup_band;
   if (out->slice_steps == 0) out->slice_steps = d.slice_steps;
+  if (out->band_lanes == 0) out->band_lanes = d.band_lanes;
 }
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
@@ -184,6 +185,8 @@ int validate_options(bh_ctx* ctx, const bh_render_options& o) {
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "setup_band must be >= 0");
   if (o.slice_steps < 4 || o.slice_steps > 4096)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
+  if (o.band_lanes < 1 || o.band_lanes > 32)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_lanes must be in [1, 32]");
   if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
   if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
@@ -309,6 +312,7 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->s2_len_f = float(d->s2_len);
   d->half_w_f = float(d->half_w);
   d->half_h_f = float(d->half_h);
+  d->inv_mass_f = float(1.0 / d->mass);
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
@@ -355,11 +359,10 @@ LaunchParams base_params(const bh_render_options& o) {
   p.format = o.format;
   p.raygen = o.raygen;
   p.max_steps = o.max_steps;
-  p.step = o.step;
-  p.u_escape = 1.0 / o.r_escape;
-  p.band = o.band;
-  p.band_step = o.band_step;
-  p.setup_band = o.setup_band;
+  p.c32 = bhgb::make_rk4_consts<float>(o.step, 1.0 / o.r_escape, o.max_steps);
+  p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
+  p.cband = bhgb::make_rk4_consts<double>(o.band_step, 1.0 / o.r_escape, o.max_steps);
+  p.setup_band = float(o.setup_band);
   {
     const double bc = 3.0 * std::sqrt(3.0);
     const double lo = bc + o.band, hi = bc - o.band;
@@ -369,13 +372,13 @@ LaunchParams base_params(const bh_render_options& o) {
   }
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;
+  p.band_lanes = o.band_lanes;
   return p;
 }
 
-uint32_t band_capacity_for(int64_t total) {
-  const int64_t cap = std::max<int64_t>(int64_t(1) << 20, total / 16);
-  return uint32_t(std::min<int64_t>(cap, total + 32));
-}
+// The band list holds one entry per ray of the call, so it cannot overflow
+// (4 bytes per ray, as much as a BGRA8 frame).
+uint32_t band_capacity_for(int64_t total) { return uint32_t(total); }
 
 int persistent_blocks(bh_ctx* ctx, const LaunchParams& p, const bh_render_options& o, int* blocks) {
   int per_sm = o.blocks_per_sm;
@@ -461,15 +464,16 @@ void bh_default_options(bh_render_options* o) {
   o->max_steps = 4000;
   o->step = 0.01;
   o->r_escape = 100.0;
-  o->band = 2e-3;
+  o->band = 5e-4;
   o->band_step = 0.01;
-  o->setup_band = 0.25;
-  o->slice_steps = 32;
+  o->setup_band = 0.1;
+  o->slice_steps = 256;
+  o->band_lanes = 32;
   o->block_x = 32;
   o->block_y = 4;
   o->threads_per_block = 256;
   o->blocks_per_sm = 0;
-  o->refill_threshold = 8;
+  o->refill_threshold = 32;
 }
 
 int bh_create(bh_ctx** out, int device) {

@@ -44,6 +44,7 @@ struct DevScene {
   float F_f[3], E0_f[3], vy_f[3], vz_f[3];
   float dc_f[3], dn_f[3], dv1_f[3], ds1_f[3], ds2_f[3], de1_f[3], de2_f[3];
   float mass_f, b_c_f, r_h_f, r_in_f, r_out_f, s1_len_f, s2_len_f, half_w_f, half_h_f;
+  float inv_mass_f;
 
   DevTexture disc_tex;
   DevTexture bg_tex;
@@ -74,6 +75,31 @@ enum : unsigned long long {
   kFlagBandQueueFull = 1ull << 0,
 };
 
+// Constants of the RK4 integration in one precision, on x = u - 1/3.
+template <typename R>
+struct Rk4Consts {
+  R h, hh, q, q2, h26, h6;  // h, h/2, h^2/4, h^2/2, h^2/6, h/6
+  R x_esc, x_hor;           // escape: x <= u_esc - 1/3; horizon: x >= 1/2 - 1/3
+  R u_esc;                  // M / r_escape
+  int32_t kmax;
+};
+
+template <typename R>
+inline Rk4Consts<R> make_rk4_consts(double h, double u_escape, int kmax) {
+  Rk4Consts<R> c;
+  c.h = R(h);
+  c.hh = R(h * 0.5);
+  c.q = R(h * h * 0.25);
+  c.q2 = R(h * h * 0.5);
+  c.h26 = R(h * h / 6.0);
+  c.h6 = R(h / 6.0);
+  c.x_esc = R(u_escape - 1.0 / 3.0);
+  c.x_hor = R(0.5 - 1.0 / 3.0);
+  c.u_esc = R(u_escape);
+  c.kmax = kmax;
+  return c;
+}
+
 struct LaunchParams {
   const DevScene* scenes;
   int32_t n_scenes;
@@ -82,11 +108,10 @@ struct LaunchParams {
   int32_t format;
   int32_t raygen;
   int32_t max_steps;
-  double step;
-  double u_escape;            // M / r_escape
-  double band;                // |b - b_c| / M below which MIXED traces in FP64
-  double band_step;           // RK4 step of the FP64 band
-  double setup_band;          // |b - b_c| / M below which MIXED sets up in FP64
+  Rk4Consts<float> c32;       // bulk step, FP32
+  Rk4Consts<double> c64;      // bulk step, FP64
+  Rk4Consts<double> cband;    // band step, FP64 (MIXED)
+  float setup_band;           // |b - b_c| / M below which MIXED takes eps from FP64
   double eps_band_lo;         // the FP64 band in terms of eps = 1/(b/M)^2 - 1/27:
   double eps_band_hi;         //   eps(b_c + band) < eps < eps(b_c - band)
   int64_t total_rays;         // persistent: sum of padded scene ray counts
@@ -95,6 +120,7 @@ struct LaunchParams {
   uint32_t band_capacity;
   int32_t refill_threshold;
   int32_t slice_steps;
+  int32_t band_lanes;
 };
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.

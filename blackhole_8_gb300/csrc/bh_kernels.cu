@@ -63,11 +63,14 @@ __device__ __forceinline__ V3<R> cross(V3<R> a, V3<R> b) {
 }
 template <typename R>
 __device__ __forceinline__ R length(V3<R> a) { return sqrt(dot(a, a)); }
+// 1/sqrt: the hardware approximation in FP32, exact division in FP64.
+__device__ __forceinline__ float rnorm(float l2) { return rsqrtf(l2); }
+__device__ __forceinline__ double rnorm(double l2) { return 1.0 / sqrt(l2); }
 // cv::normalize semantics: v * (1/|v|), zero vector stays zero.
 template <typename R>
 __device__ __forceinline__ V3<R> normalize(V3<R> a) {
-  const R l = length(a);
-  const R k = l != R(0) ? R(1) / l : R(0);
+  const R l2 = dot(a, a);
+  const R k = l2 != R(0) ? rnorm(l2) : R(0);
   return a * k;
 }
 template <typename R, typename S>
@@ -339,28 +342,14 @@ __device__ Hit trace_ref(const DevScene& s, int x, int y) {
 }
 
 // ---------------------------------------------------------------------------
-// RK4 in phi on x'' = x + 3 x^2, x = M/r - 1/3.
+// RK4 in phi on x'' = x + 3 x^2, x = M/r - 1/3 (constants: Rk4Consts,
+// precomputed on the host so that the FP32 paths issue no FP64 instruction).
 template <typename R>
-struct Rk4Consts {
-  R h, hh, q, q2, h26, h6;  // h, h/2, h^2/4, h^2/2, h^2/6, h/6
-  R x_esc, x_hor;           // escape: x <= M/r_esc - 1/3; horizon: x >= 1/2 - 1/3
-  int kmax;
-};
-
-template <typename R>
-__device__ __forceinline__ Rk4Consts<R> rk4_consts(double h, double u_escape, int kmax) {
-  Rk4Consts<R> c;
-  c.h = R(h);
-  c.hh = R(h * 0.5);
-  c.q = R(h * h * 0.25);
-  c.q2 = R(h * h * 0.5);
-  c.h26 = R(h * h / 6.0);
-  c.h6 = R(h / 6.0);
-  c.x_esc = R(u_escape - 1.0 / 3.0);
-  c.x_hor = R(0.5 - 1.0 / 3.0);
-  c.kmax = kmax;
-  return c;
-}
+__device__ __forceinline__ const Rk4Consts<R>& bulk_consts(const LaunchParams& p);
+template <>
+__device__ __forceinline__ const Rk4Consts<float>& bulk_consts<float>(const LaunchParams& p) { return p.c32; }
+template <>
+__device__ __forceinline__ const Rk4Consts<double>& bulk_consts<double>(const LaunchParams& p) { return p.c64; }
 
 template <typename R>
 __device__ __forceinline__ R fx(R x) { return x * fma(R(3), x, R(1)); }
@@ -426,39 +415,47 @@ struct RayState {
 };
 
 // Sets up the RK4 state from a plane ray computed in precision RS.
-template <typename R, typename RS>
-__device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<RS>& ray, double h, RayState<R>& st) {
-  const RS M = RS(s.mass);
-  st.yv = cast3<R>(ray.yv);
-  st.xv = cast3<R>(ray.xv);
+template <typename R>
+__device__ __forceinline__ R inv_mass(const DevScene& s);
+template <>
+__device__ __forceinline__ float inv_mass<float>(const DevScene& s) { return s.inv_mass_f; }
+template <>
+__device__ __forceinline__ double inv_mass<double>(const DevScene& s) { return 1.0 / s.mass; }
+
+// Sets up the RK4 state of a plane ray; everything in precision R.
+template <typename R>
+__device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& ray, R h, RayState<R>& st) {
+  const R M = BH_S(R, s, mass);
+  st.yv = ray.yv;
+  st.xv = ray.xv;
   st.k = 0;
   st.kc = 0x7fffffff;
   st.dcr = R(0);
   st.ev = R(0);
-  const RS r0 = sqrt(ray.F0 * ray.F0 + ray.F1 * ray.F1 + ray.b * ray.b);
-  const RS bm = ray.b / M;
-  const RS x0 = M / r0 - RS(1.0 / 3.0);
-  const RS phi0 = atan2(ray.b, ray.F1);
-  st.x = R(x0);
-  st.phi0 = R(phi0);
-  if (!(bm > RS(1e-6))) {  // heads into the centre
+  const R bm = ray.b * inv_mass<R>(s);
+  const R x0 = M * rnorm(ray.F0 * ray.F0 + ray.F1 * ray.F1 + ray.b * ray.b) - R(1.0 / 3.0);
+  const R phi0 = atan2(ray.b, ray.F1);
+  st.x = x0;
+  st.phi0 = phi0;
+  if (!(bm > R(1e-6))) {  // heads into the centre
     st.status = kHorizon;
     st.w = R(0);
     st.eps = R(0);
     return;
   }
-  const RS eps = RS(1) / (bm * bm) - RS(1.0 / 27.0);
-  st.eps = R(eps);
-  st.w = R(copysign(sqrt(fmax(eps + x0 * x0 * fma(RS(2), x0, RS(1)), RS(0))), ray.F1));
+  const R mb = M / ray.b;
+  const R eps = mb * mb - R(1.0 / 27.0);
+  st.eps = eps;
+  st.w = copysign(sqrt(fmax(eps + x0 * x0 * fma(R(2), x0, R(1)), R(0))), ray.F1);
   st.status = kRunning;
   if (s.disc_on) {
-    const V3<RS> n = BH_V(RS, s, dn);
-    const RS A = dot(n, ray.yv), B = dot(n, ray.xv);
-    if (A * A + B * B > RS(1e-24)) {
-      RS d = fmod(atan2(B, A) + kPi<RS>() * RS(0.5) - phi0, kPi<RS>());
-      if (d <= RS(0)) d += kPi<RS>();
-      st.dcr = R(d);
-      st.kc = (int)floor(d / RS(h));
+    const V3<R> n = BH_V(R, s, dn);
+    const R A = dot(n, ray.yv), B = dot(n, ray.xv);
+    if (A * A + B * B > R(1e-24)) {
+      R d = fmod(atan2(B, A) + kPi<R>() * R(0.5) - phi0, kPi<R>());
+      if (d <= R(0)) d += kPi<R>();
+      st.dcr = d;
+      st.kc = (int)floor(d / h);
     }
   }
 }
@@ -582,14 +579,16 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
 
 // Shades a finished RK4 ray.
 template <typename R>
-__device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c, double u_escape) {
+__device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c) {
   Hit hit = {make_uchar4(0, 0, 0, 255), BH_CLASS_HORIZON, 0.f};
   if (st.status == kMaxSteps) {
     hit.cls = BH_CLASS_MAXSTEPS;
   } else if (st.status == kDisc) {
     const R phic = st.phi0 + st.dcr;
     const R rw = BH_S(R, s, mass) / st.ev;
-    const V3<R> p = st.yv * (rw * cos(phic)) + st.xv * (rw * sin(phic));
+    R sp, cp;
+    sincos(phic, &sp, &cp);
+    const V3<R> p = st.yv * (rw * cp) + st.xv * (rw * sp);
     hit.cls = BH_CLASS_DISC;
     hit.aux = float(R(1) / st.ev);
     hit.bgra = disc_color(s, p);
@@ -599,7 +598,7 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     const R xa = st.xa, xb = st.x, ha = c.h * st.wa, hb = c.h * st.w, xe = c.x_esc;
     R t = (xa - xe) / (xa - xb);
     t = fmin(fmax(t, R(0)), R(1));
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < (sizeof(R) == 4 ? 2 : 3); ++i) {
       const R t2 = t * t, t3 = t2 * t;
       const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha +
                   (R(3) * t2 - R(2) * t3) * xb + (t3 - t2) * hb;
@@ -612,11 +611,16 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
                  (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
     const R we = dp / c.h;
     const R phie = st.phi0 + (R(st.k - 1) + t) * c.h;
-    const R psi = phie + atan2(R(u_escape), -we);
+    // direction angle psi = phie + atan2(u, -w) (from the radial direction,
+    // measured from yv toward xv); its cosine and sine without atan2
     hit.cls = BH_CLASS_MISS;
-    hit.aux = float(psi - kPi<R>());
+    if (s.aux) hit.aux = float(phie + atan2(c.u_esc, -we) - kPi<R>());
     if (s.has_bg) {
-      const V3<R> d = st.yv * cos(psi) + st.xv * sin(psi);
+      R sp, cp;
+      sincos(phie, &sp, &cp);
+      const R k = rnorm(we * we + c.u_esc * c.u_esc);
+      const R cd = -we * k, sd = c.u_esc * k;
+      const V3<R> d = st.yv * (cp * cd - sp * sd) + st.xv * (sp * cd + cp * sd);
       hit.bgra = background_color(s, d);
     }
   }
@@ -629,18 +633,17 @@ constexpr double kBC = 5.196152422706632;  // 3 sqrt(3)
 
 // Full trace in one precision R.
 template <typename R, bool kMixed>
-__device__ Hit trace_rk4(const DevScene& s, int x, int y, double h, double u_escape, int kmax, int* steps) {
-  const Rk4Consts<R> c = rk4_consts<R>(h, u_escape, kmax);
+__device__ Hit trace_rk4(const DevScene& s, int x, int y, const Rk4Consts<R>& c, int* steps) {
   RayState<R> st;
-  init_rk4<R, R>(s, make_ray<R>(s, x, y), h, st);
+  init_rk4<R>(s, make_ray<R>(s, x, y), c.h, st);
   *steps = advance_rk4<R, kMixed>(s, st, c, 0x7fffffff);
-  return finish_rk4<R>(s, st, c, u_escape);
+  return finish_rk4<R>(s, st, c);
 }
 
 // FP64 trace of a band ray (out of line: keeps FP64 register pressure away
 // from the FP32 callers).
 __device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
-  return trace_rk4<double, false>(s, x, y, p.band_step, p.u_escape, p.max_steps, steps);
+  return trace_rk4<double, false>(s, x, y, p.cband, steps);
 }
 
 // First integral eps = 1/(b/M)^2 - 1/27 of pixel (x, y) in FP64:
@@ -661,8 +664,8 @@ __device__ __noinline__ double eps_fp64(const DevScene& s, int x, int y) {
 __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, const LaunchParams& p,
                                             RayState<float>& st) {
   const PlaneRay<float> r = make_ray<float>(s, x, y);
-  init_rk4<float, float>(s, r, p.step, st);
-  if (fabsf(r.b / s.mass_f - float(kBC)) < float(p.setup_band)) {
+  init_rk4<float>(s, r, p.c32.h, st);
+  if (fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band) {
     const double eps = eps_fp64(s, x, y);
     if (eps > p.eps_band_lo && eps < p.eps_band_hi) return false;
     if (st.status == kRunning) {
@@ -694,19 +697,18 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
     h = p.precision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
   } else if (p.precision == BH_PRECISION_FP64) {
-    h = trace_rk4<double, false>(s, x, y, p.step, p.u_escape, p.max_steps, &steps);
+    h = trace_rk4<double, false>(s, x, y, p.c64, &steps);
   } else if (p.precision == BH_PRECISION_MIXED) {
     RayState<float> st;
     if (setup_mixed(s, x, y, p, st)) {
-      const Rk4Consts<float> c = rk4_consts<float>(p.step, p.u_escape, p.max_steps);
-      steps = advance_rk4<float, true>(s, st, c, 0x7fffffff);
-      h = finish_rk4<float>(s, st, c, p.u_escape);
+      steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
+      h = finish_rk4<float>(s, st, p.c32);
     } else {
       band_ray = 1;
       h = trace_band(s, x, y, p, &steps);
     }
   } else {
-    h = trace_rk4<float, false>(s, x, y, p.step, p.u_escape, p.max_steps, &steps);
+    h = trace_rk4<float, false>(s, x, y, p.c32, &steps);
   }
   store_hit(s, p.format, x, y, h);
   if (p.counters) {
@@ -763,23 +765,14 @@ __device__ __forceinline__ bool take_fp32_ray(const LaunchParams& p, int scene, 
   const DevScene& s = p.scenes[scene];
   if (!ray_pixel(s, item - s.ray_begin, px, py)) return false;
   if (!kMixed) {
-    init_rk4<float, float>(s, make_ray<float>(s, *px, *py), p.step, st);
+    init_rk4<float>(s, make_ray<float>(s, *px, *py), p.c32.h, st);
     return true;
   }
   if (setup_mixed(s, *px, *py, p, st)) return true;
+  // deferred to the FP64 pass; the list has one slot per ray of the call
   const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
-  if (slot < p.band_capacity) {
-    p.band_list[slot] = (uint32_t)item;
-  } else {  // list full: trace inline in FP64
-    atomicAdd(&p.counters->band_overflow, 1ull);
-    int bsteps = 0;
-    const Hit hb = trace_band(s, *px, *py, p, &bsteps);
-    store_hit(s, p.format, *px, *py, hb);
-    atomicAdd(&p.counters->band_rays, 1ull);
-    atomicAdd(&p.counters->band_steps, (unsigned long long)bsteps);
-    atomicAdd(&p.counters->rays, 1ull);
-    *steps += bsteps;
-  }
+  if (slot < p.band_capacity) p.band_list[slot] = (uint32_t)item;
+  else atomicOr(&p.counters->flags, kFlagBandQueueFull);
   return false;
 }
 
@@ -789,8 +782,10 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
   using R = typename std::conditional<kPass == 2, double, float>::type;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1;
-  const double h = kPass == 2 ? p.band_step : p.step;
-  const Rk4Consts<R> c = rk4_consts<R>(h, p.u_escape, p.max_steps);
+  Rk4Consts<R> c;
+  if constexpr (kPass == 2) c = p.cband;
+  else c = p.c32;
+  const R h = c.h;
   const long long n_items =
       kPass == 2 ? (long long)min(*(volatile unsigned long long*)&p.counters->band_count,
                                   (unsigned long long)p.band_capacity)
@@ -800,22 +795,26 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
   st.status = kDone;
   int scene = 0, px = 0, py = 0;
   unsigned long long steps = 0, rays = 0;
-  const int thr = max(1, min(32, p.refill_threshold));
-  long long pend_base = 0;  // first item index of the pending 32
+  // The FP64 pass can leave lanes unused: FP64 issue is the bottleneck there,
+  // and fewer band rays per warp spread them over more warps and SMs.
+  const int chunk = kPass == 2 ? max(1, min(32, p.band_lanes)) : 32;
+  const unsigned usable = chunk == 32 ? kFull : ((1u << chunk) - 1u);
+  const int thr = max(1, min(chunk, p.refill_threshold));
+  long long pend_base = 0;  // first item index of the pending chunk
   unsigned pend_mask = 0;   // its items not yet handed out
   int pend_scene = 0;
   bool exhausted = false;
 
   for (;;) {
-    unsigned idle = __ballot_sync(kFull, st.status == kDone);
-    if (idle == kFull && exhausted && pend_mask == 0) break;
-    if (__popc(idle) >= thr || idle == kFull) {
+    unsigned idle = __ballot_sync(kFull, st.status == kDone) & usable;
+    if (idle == usable && exhausted && pend_mask == 0) break;
+    if (__popc(idle) >= thr || idle == usable) {
       // hand out pending items until every lane is busy or work runs out
       while (idle) {
         if (pend_mask == 0) {
           if (exhausted) break;
           unsigned long long t = 0;
-          if (lane == 0) t = atomicAdd(queue, 32ull);
+          if (lane == 0) t = atomicAdd(queue, (unsigned long long)chunk);
           t = __shfl_sync(kFull, t, 0);
           if ((long long)t >= n_items) {
             exhausted = true;
@@ -823,7 +822,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
           }
           pend_base = (long long)t;
           const long long left = n_items - pend_base;
-          pend_mask = left >= 32 ? kFull : ((1u << left) - 1u);
+          pend_mask = left >= chunk ? usable : ((1u << left) - 1u);
           if constexpr (kPass != 2) {
             int sc = 0;
             if (lane == 0) sc = find_scene(p, pend_base);
@@ -840,7 +839,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
             const DevScene& s = p.scenes[scene];
             if (ray_pixel(s, ray - s.ray_begin, &px, &py)) {
               ++rays;
-              init_rk4<R, R>(s, make_ray<R>(s, px, py), h, st);
+              init_rk4<R>(s, make_ray<R>(s, px, py), h, st);
             }
           } else {
             scene = pend_scene;
@@ -848,14 +847,14 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
           }
         }
         for (int i = 0; i < n; ++i) pend_mask &= pend_mask - 1u;  // drop the n lowest items
-        idle = __ballot_sync(kFull, st.status == kDone);
+        idle = __ballot_sync(kFull, st.status == kDone) & usable;
       }
     }
     if (st.status != kDone) {
       const DevScene& s = p.scenes[scene];
       steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
       if (st.status != kRunning) {
-        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c, p.u_escape));
+        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c));
         st.status = kDone;
       }
     }

@@ -149,20 +149,22 @@ typedef struct bh_render_options {
   double step;               /* RK4 step in phi (default 0.01) */
   double r_escape;           /* RK4 escape radius in units of M (default 100) */
   double band;               /* MIXED: rays with |b - 3 sqrt(3) M| < band * M are
-                                traced in FP64 with step band_step (default 2e-3) */
+                                traced in FP64 with step band_step (default 5e-4) */
   int32_t block_x;           /* GRID block shape (default 32 x 4) */
   int32_t block_y;
   int32_t threads_per_block; /* PERSISTENT block size (default 256) */
   int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
   int32_t refill_threshold;  /* PERSISTENT: refill a warp once this many lanes
-                                are idle (default 8) */
+                                are idle (default 32) */
   double band_step;          /* MIXED: RK4 step of the FP64 band (default 0.01) */
   double setup_band;         /* MIXED: rays with |b - 3 sqrt(3) M| < setup_band * M
-                                get their impact parameter, conserved energy and
-                                plane basis from FP64 ray setup (default 0.25) */
+                                take their first integral 1/b^2 - 1/27 from FP64
+                                (default 0.1) */
   int32_t slice_steps;       /* PERSISTENT: integration steps between refill
-                                checks (default 32) */
-  int32_t reserved[5];
+                                checks (default 256) */
+  int32_t band_lanes;        /* MIXED + PERSISTENT: lanes per warp that trace
+                                FP64 band rays (1..32, default 32) */
+  int32_t reserved[4];
 } bh_render_options;
 
 /* Counters of the most recent render on a context. */
@@ -171,7 +173,8 @@ typedef struct bh_render_stats {
   uint64_t steps;         /* integration steps summed over rays */
   uint64_t band_rays;     /* rays traced in FP64 because of the band */
   uint64_t band_steps;    /* steps of those rays */
-  uint64_t band_overflow; /* band rays traced inline (deferral list full) */
+  uint64_t band_overflow; /* band rays that found no slot in the band list
+                             (0: the list holds one slot per ray) */
   uint64_t flags;         /* device error bits (0 = none) */
   double kernel_ms;       /* device time of the launches, CUDA events */
   uint64_t h2d_bytes;     /* bytes copied host -> device by the call */
