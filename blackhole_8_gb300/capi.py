@@ -135,3 +135,14 @@ def default_options(**overrides) -> RenderOptions:
             raise AttributeError(f"no render option {k!r}")
         setattr(o, k, v)
     return o
+
+
+class DeviceTexture(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+SIGNATURES["bh_render_noalloc"] = (C.c_int, [C.c_int, C.POINTER(Scene), C.c_int32, C.POINTER(DeviceTexture),
+                                             C.c_int32, C.POINTER(Frame), C.POINTER(RenderOptions), C.c_void_p,
+                                             C.c_char_p, C.c_int32])
+NOALLOC_MAX_SCENES = 64
+NOALLOC_MAX_RAYS = 4000000

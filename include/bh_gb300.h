@@ -228,6 +228,35 @@ int bh_sequence_launch(bh_sequence* seq, void* stream);
 int bh_sequence_stats(bh_sequence* seq, bh_render_stats* out);
 void bh_sequence_destroy(bh_sequence* seq);
 
+/* ---- render without allocating -------------------------------------------------
+ * No counterpart in the reference (it renders on the CPU and never allocates
+ * device memory). For callers that may not allocate at render time -- a
+ * real-time frame loop with a fixed memory budget, or a host that gives the
+ * library only pre-allocated device buffers -- and so cannot use bh_render or
+ * bh_render_device, whose contexts grow their buffers with cudaMalloc.
+ * Textures (BGRA8, caller-owned device memory, indexed by the scenes'
+ * texture ids) and frames are in device memory; scenes are on the host. The
+ * library's own scratch (counters, scene records, the FP64 band list) lives
+ * in one fixed device array of about 16 MiB that every device loading the
+ * library holds until exit; calls are limited to BH_NOALLOC_MAX_SCENES scenes
+ * and BH_NOALLOC_MAX_RAYS rays (scenes padded to 8x4 tiles) and are rejected
+ * with BH_ERR_INVALID_ARGUMENT above that. The first call on a device takes
+ * the array's address (make it before any stream capture). All calls share
+ * the array: calls whose work overlaps on the GPU race. Enqueued on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream); returns without
+ * waiting. `error` (may be NULL) receives a message of at most error_len
+ * bytes. */
+#define BH_NOALLOC_MAX_SCENES 64
+#define BH_NOALLOC_MAX_RAYS 4000000
+typedef struct bh_device_texture {
+  const void* texels;  /* width*height BGRA8 texels in device memory */
+  int32_t width;
+  int32_t height;
+} bh_device_texture;
+int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, const bh_device_texture* textures,
+                      int32_t n_textures, const bh_frame* frames, const bh_render_options* opts, void* stream,
+                      char* error, int32_t error_len);
+
 /* ---- device probes ------------------------------------------------------------
  * Measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops) and its
  * multiprocessor count; used as the roofline denominator. */
