@@ -146,3 +146,13 @@ SIGNATURES["bh_render_noalloc"] = (C.c_int, [C.c_int, C.POINTER(Scene), C.c_int3
                                              C.c_char_p, C.c_int32])
 NOALLOC_MAX_SCENES = 64
 NOALLOC_MAX_RAYS = 4000000
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("step", C.c_double), ("max_deflection", C.c_double), ("max_radius_error", C.c_double),
+                ("class_mismatch", C.c_double), ("kernel_ms", C.c_double), ("candidates", C.c_int32),
+                ("from_cache", C.c_int32)]
+
+
+SIGNATURES["bh_autotune"] = (C.c_int, [C.c_void_p, C.POINTER(Scene), C.c_int32, C.POINTER(RenderOptions),
+                                       C.c_double, C.c_char_p, C.POINTER(TuneReport)])

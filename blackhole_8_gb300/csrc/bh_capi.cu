@@ -812,6 +812,242 @@ void bh_sequence_destroy(bh_sequence* q) {
   delete q;
 }
 
+// ---- autotuner --------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Device buffers owned by one tuning run.
+struct TuneBuffers {
+  std::vector<void*> ptrs;
+  ~TuneBuffers() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  void* get(size_t bytes, cudaError_t* e) {
+    void* p = nullptr;
+    *e = cudaMalloc(&p, bytes);
+    if (*e == cudaSuccess) ptrs.push_back(p);
+    return p;
+  }
+};
+
+struct SampleOut {
+  std::vector<uint8_t> cls;
+  std::vector<float> aux;
+};
+
+// Renders the sample scenes with `o` into device frames and copies class and
+// aux back.
+int render_sample(bh_ctx* ctx, const std::vector<bh_scene>& s, const std::vector<bh_frame>& f,
+                  const bh_render_options& o, std::vector<SampleOut>* out) {
+  int rc = render_on_device(ctx, s.data(), int32_t(s.size()), f.data(), o, ctx->stream);
+  if (rc) return rc;
+  out->resize(s.size());
+  for (size_t i = 0; i < s.size(); ++i) {
+    const size_t px = size_t(s[i].camera.width) * s[i].camera.height;
+    (*out)[i].cls.resize(px);
+    (*out)[i].aux.resize(px);
+    BH_CUDA(ctx, cudaMemcpyAsync((*out)[i].cls.data(), f[i].hit_class, px, cudaMemcpyDeviceToHost, ctx->stream));
+    BH_CUDA(ctx, cudaMemcpyAsync((*out)[i].aux.data(), f[i].aux, px * sizeof(float), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  }
+  BH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return BH_OK;
+}
+
+void compare_sample(const std::vector<SampleOut>& ref, const std::vector<SampleOut>& got, double* defl,
+                    double* radius, double* mismatch) {
+  size_t total = 0, bad = 0;
+  double d = 0, r = 0;
+  for (size_t i = 0; i < ref.size(); ++i) {
+    for (size_t k = 0; k < ref[i].cls.size(); ++k) {
+      ++total;
+      if (ref[i].cls[k] != got[i].cls[k]) {
+        ++bad;
+        continue;
+      }
+      const double e = std::fabs(double(ref[i].aux[k]) - double(got[i].aux[k]));
+      if (ref[i].cls[k] == BH_CLASS_MISS) d = std::max(d, e);
+      else if (ref[i].cls[k] == BH_CLASS_DISC) r = std::max(r, e);
+    }
+  }
+  *defl = d;
+  *radius = r;
+  *mismatch = total ? double(bad) / double(total) : 0.0;
+}
+
+std::string tune_key(bh_ctx* ctx, const bh_scene* scenes, int32_t n, double max_error) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, ctx->device);
+  int64_t rays = 0;
+  for (int i = 0; i < n; ++i) rays += padded_rays(scenes[i].camera);
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s|sms=%d|n=%d|rays=%lld|w=%d|h=%d|err=%.3g", prop.name, ctx->sm_count, n,
+                (long long)rays, scenes[0].camera.width, scenes[0].camera.height, max_error);
+  for (char* c = buf; *c; ++c)
+    if (*c == ' ') *c = '_';
+  return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& key, bh_render_options* o, bh_tune_report* rep) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  while (std::fgets(line, sizeof(line), f)) {
+    char k[600];
+    double step, band, defl, rad, mis, ms;
+    int threads, refill, slice;
+    if (std::sscanf(line, "%599s %lf %lf %d %d %d %lf %lf %lf %lf", k, &step, &band, &threads, &refill, &slice,
+                    &defl, &rad, &mis, &ms) == 10 &&
+        key == k) {
+      o->step = step;
+      o->band = band;
+      o->threads_per_block = threads;
+      o->refill_threshold = refill;
+      o->slice_steps = slice;
+      rep->step = step;
+      rep->max_deflection = defl;
+      rep->max_radius_error = rad;
+      rep->class_mismatch = mis;
+      rep->kernel_ms = ms;
+      found = true;  // the last matching line wins
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void cache_store(const char* path, const std::string& key, const bh_render_options& o, const bh_tune_report& rep) {
+  if (!path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%s %.17g %.17g %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), o.step, o.band,
+               o.threads_per_block, o.refill_threshold, o.slice_steps, rep.max_deflection, rep.max_radius_error,
+               rep.class_mismatch, rep.kernel_ms);
+  std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_options* opts, double max_error,
+                const char* cache_path, bh_tune_report* report) {
+  if (!ctx || !opts || !report) return BH_ERR_INVALID_ARGUMENT;
+  if (!(max_error > 0)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "max_error must be positive");
+  *report = bh_tune_report{};
+  bh_render_options base;
+  resolve_defaults(opts, &base);
+  if (base.integrator != BH_INTEGRATOR_RK4)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "the autotuner tunes the RK4 tracer");
+  base.precision = BH_PRECISION_MIXED;
+  base.schedule = BH_SCHEDULE_PERSISTENT;
+  // validate the batch once (frames are the tuner's own)
+  {
+    std::vector<bh_frame> dummy(size_t(n > 0 ? n : 1), bh_frame{reinterpret_cast<void*>(1), nullptr, nullptr});
+    bh_render_options chk;
+    int rc = check_inputs(ctx, scenes, n, dummy.data(), &base, &chk);
+    if (rc) return rc;
+  }
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  const std::string key = tune_key(ctx, scenes, n, max_error);
+  bh_render_options chosen = base;
+  if (cache_lookup(cache_path, key, &chosen, report)) {
+    report->from_cache = 1;
+    *opts = chosen;
+    return BH_OK;
+  }
+
+  TuneBuffers mem;
+  cudaError_t e = cudaSuccess;
+  // sample: up to 4 scenes, evenly spaced, with class and aux outputs
+  std::vector<bh_scene> sample;
+  const int ns = std::min<int32_t>(n, 4);
+  for (int i = 0; i < ns; ++i) sample.push_back(scenes[ns == 1 ? 0 : int64_t(i) * (n - 1) / (ns - 1)]);
+  std::vector<bh_frame> sf(sample.size());
+  for (size_t i = 0; i < sample.size(); ++i) {
+    const size_t px = size_t(sample[i].camera.width) * sample[i].camera.height;
+    sf[i].pixels = mem.get(px * 4, &e);
+    if (e == cudaSuccess) sf[i].hit_class = static_cast<uint8_t*>(mem.get(px, &e));
+    if (e == cudaSuccess) sf[i].aux = static_cast<float*>(mem.get(px * sizeof(float), &e));
+    if (e != cudaSuccess) return cuda_err(ctx, e, "tuner sample buffers");
+  }
+  std::vector<SampleOut> ref, got;
+  bh_render_options ro = base;
+  ro.precision = BH_PRECISION_FP64;
+  ro.schedule = BH_SCHEDULE_GRID;
+  ro.format = BH_FORMAT_BGRA8;
+  int rc = render_sample(ctx, sample, sf, ro, &ref);
+  if (rc) return rc;
+
+  // 1) the largest step that keeps the sample within max_error / 2
+  std::vector<double> steps;
+  for (double h : {0.1, 0.08, 0.05, 0.04, 0.03, 0.02})
+    if (h > base.step) steps.push_back(h);
+  steps.push_back(base.step);  // the reference step itself is the last resort
+  bool ok = false;
+  for (double h : steps) {
+    bh_render_options c = base;
+    c.step = h;
+    c.format = BH_FORMAT_BGRA8;
+    if ((rc = render_sample(ctx, sample, sf, c, &got))) return rc;
+    report->candidates++;
+    double d, r, m;
+    compare_sample(ref, got, &d, &r, &m);
+    if (d <= 0.5 * max_error && m <= 1e-4) {
+      chosen.step = h;
+      report->step = h;
+      report->max_deflection = d;
+      report->max_radius_error = r;
+      report->class_mismatch = m;
+      ok = true;
+      break;
+    }
+  }
+  if (!ok) return set_err(ctx, BH_ERR_UNSUPPORTED, "no candidate step meets the deflection bound");
+
+  // 2) the fastest schedule on the whole batch (pixels only)
+  std::vector<bh_frame> bf(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) {
+    bf[i].pixels = mem.get(size_t(scenes[i].camera.width) * scenes[i].camera.height * 4, &e);
+    bf[i].hit_class = nullptr;
+    bf[i].aux = nullptr;
+    if (e != cudaSuccess) return cuda_err(ctx, e, "tuner batch buffers");
+  }
+  double best = 1e30;
+  bh_render_options best_o = chosen;
+  for (double band : {5e-4, 1e-3})
+    for (int threads : {128, 256})
+      for (int refill : {16, 32})
+        for (int slice : {128, 256, 512}) {
+          bh_render_options c = chosen;
+          c.band = std::max(band, base.band);
+          c.threads_per_block = threads;
+          c.refill_threshold = refill;
+          c.slice_steps = slice;
+          c.format = BH_FORMAT_BGRA8;
+          double ms = 1e30;
+          for (int rep = 0; rep < 2; ++rep) {
+            if ((rc = render_on_device(ctx, scenes, n, bf.data(), c, ctx->stream))) return rc;
+            bh_render_stats st;
+            if ((rc = bh_get_stats(ctx, &st))) return rc;
+            ms = std::min(ms, st.kernel_ms);
+          }
+          report->candidates++;
+          if (ms < best) {
+            best = ms;
+            best_o = c;
+          }
+        }
+  best_o.format = opts->format;
+  report->kernel_ms = best;
+  *opts = best_o;
+  cache_store(cache_path, key, best_o, *report);
+  return BH_OK;
+}
+
 // ---- probes ----------------------------------------------------------------------
 int bh_probe_fp32_peak(bh_ctx* ctx, double* tflops, int32_t* sm_count) {
   if (!ctx || !tflops) return BH_ERR_INVALID_ARGUMENT;

@@ -134,6 +134,19 @@ class Renderer:
         _check(self.lib, self.ctx, rc)
         return Sequence(self, h, len(c_scenes))
 
+    # -- autotuner ---------------------------------------------------------------------------
+    def autotune(self, c_scenes, options: capi.RenderOptions | None = None, max_error: float = 1e-4,
+                 cache_path: str | None = None) -> tuple[capi.RenderOptions, capi.TuneReport]:
+        """bh_autotune: the mixed batched tracer's step and schedule for a batch."""
+        opts = options or capi.default_options()
+        out = capi.RenderOptions()
+        C.memmove(C.byref(out), C.byref(opts), C.sizeof(out))
+        rep = capi.TuneReport()
+        rc = self.lib.bh_autotune(self.ctx, c_scenes, len(c_scenes), C.byref(out), max_error,
+                                  cache_path.encode() if cache_path else None, C.byref(rep))
+        _check(self.lib, self.ctx, rc)
+        return out, rep
+
     # -- probes ---------------------------------------------------------------------------
     def fp32_peak(self) -> tuple[float, int]:
         t = C.c_double()

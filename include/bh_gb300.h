@@ -228,6 +228,34 @@ int bh_sequence_launch(bh_sequence* seq, void* stream);
 int bh_sequence_stats(bh_sequence* seq, bh_render_stats* out);
 void bh_sequence_destroy(bh_sequence* seq);
 
+/* ---- autotuner -----------------------------------------------------------------------
+ * No counterpart in the reference. Chooses the mixed-precision batched
+ * tracer's RK4 step, FP64 band width and persistent-schedule shape (block
+ * size, refill threshold, slice length) for a batch of scenes:
+ *   1. renders a sample of the scenes (up to 4, evenly spaced) in FP64 with
+ *      the options' step as the reference (the oracle's scheme);
+ *   2. takes the largest step in {0.1, 0.08, 0.05, 0.04, 0.03, 0.02, 0.01}
+ *      whose MIXED render of the sample stays within max_error / 2 rad of the
+ *      reference deflection on every escaped ray with an agreeing class, with
+ *      classes agreeing on >= 99.99 % of pixels;
+ *   3. times the schedule candidates on the whole batch and keeps the fastest.
+ * `opts` is read as the base (integrator must be RK4) and overwritten with
+ * the choice (precision MIXED, schedule PERSISTENT). When cache_path is not
+ * NULL the choice is looked up there first (key: device, batch shape,
+ * max_error) and appended after tuning. The sample's renders and the timing
+ * frames use the context's device buffers. */
+typedef struct bh_tune_report {
+  double step;             /* chosen RK4 step */
+  double max_deflection;   /* max |deflection - FP64 reference| at that step (rad) */
+  double max_radius_error; /* max |disc hit radius - FP64 reference| (units of M) */
+  double class_mismatch;   /* fraction of sample pixels whose class differs */
+  double kernel_ms;        /* device time of the chosen configuration on the batch */
+  int32_t candidates;      /* configurations rendered */
+  int32_t from_cache;      /* 1 when the choice came from the cache file */
+} bh_tune_report;
+int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_options* opts, double max_error,
+                const char* cache_path, bh_tune_report* report);
+
 /* ---- render without allocating -------------------------------------------------
  * No counterpart in the reference (it renders on the CPU and never allocates
  * device memory). For callers that may not allocate at render time -- a
