@@ -3,17 +3,19 @@
 A step is one pass of the tracer over the whole fly-through (120 frames of
 1920x1080 = 248.8 M rays), replayed as one captured CUDA graph. Lines:
 
-- ``value``: the mixed-precision batched tracer (persistent work-stealing
-  launch over all 120 frames, FP32 bulk, FP64 for rays within the band of
-  the critical impact parameter and for disc-crossing refinement),
-  device-resident inputs, L2 flushed between timed steps.
-- ``variants.plain_fp32``: the plain FP32 tracer (one thread per pixel).
-- ``e2e``: the same mixed tracer through the C ABI's bh_render with host
+- ``value``: the mixed-precision batched tracer with the autotuner's choice
+  (bh_autotune: the largest RK4 step whose render stays within half the
+  1e-4 rad deflection bound of an FP64 reference render, then the fastest
+  persistent schedule). FP32 bulk, FP64 first integral near b_c, FP64 band,
+  FP64 refinement of crossings near disc edges. Inputs resident, L2 flushed
+  between timed steps.
+- ``variants``: the mixed tracer at the spec's step 0.01 (equal work), and the
+  plain FP32 tracer (step 0.01) in both schedules.
+- ``e2e``: the tuned mixed tracer through the C ABI's bh_render with host
   buffers: scene upload, render and the BGR8 (CV_8UC3) frames copied back to
   pinned host memory inside the timed region.
 - ``cpu_baseline``: the reference's own render loop (oracle/_ref, its
-  20+20-step trapezoid scheme, FP64) on the host cores, on a bounded sample of
-  the same fly-through.
+  20+20-step trapezoid scheme, FP64) on all host cores, on 8 of the 120 frames.
 
 ``--impl reference`` times only that reference CPU render (rank 0).
 Multi-GPU: every rank renders its own copy of the fly-through (replicas, no
@@ -23,7 +25,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -35,9 +36,10 @@ sys.path.insert(0, ROOT)
 
 FRAMES, WIDTH, HEIGHT = 120, 1920, 1080
 METRIC = "geodesic Mrays/s 1080p, plain vs mixed-prec batched @<=1e-4 rad; adjoint Mrays/s"
-WORKLOAD = "fly-through 120 frames 1920x1080, r 30M->8M spiral, incl 60->89 deg, FoV 60 deg, RK4 dphi=0.01, " \
-           "<=4000 steps, escape 100M"
+WORKLOAD = "fly-through 120 frames 1920x1080, r 30M->8M spiral, incl 60->89 deg, FoV 60 deg, disc 6-20M, " \
+           "RK4 <=4000 steps, escape 100M"
 CPU_SAMPLE_FRAMES = list(range(0, FRAMES, 15))  # 8 frames
+MAX_DEFLECTION_ERROR = 1e-4
 
 
 def parse():
@@ -52,13 +54,10 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-# ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
 
@@ -76,9 +75,8 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except (OSError, FileNotFoundError):
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
             self.proc = None
 
     def _read(self):
@@ -93,7 +91,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, watts, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -102,6 +100,7 @@ class ClockSampler:
             try:
                 sm.append(float(f[1]))
                 smax.append(float(f[2]))
+                watts.append(float(f[3]))
             except ValueError:
                 continue
             for n, v in zip(names, f[5:9]):
@@ -111,36 +110,33 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(watts) if watts else None}
 
 
-# ---------------------------------------------------------------------------
 def cpu_reference(scenes, frames_idx, threads: int):
     """The reference's own render loop on the host cores; falls back to the
     oracle's restatement of it. Returns (Mrays/s, threads, kind, sample)."""
     from oracle import oracle, refbridge
     sample = [scenes[i] for i in frames_idx]
-    desc = f"{len(sample)} of {len(scenes)} fly-through frames ({frames_idx[0]}..{frames_idx[-1]} step " \
-           f"{frames_idx[1] - frames_idx[0] if len(frames_idx) > 1 else 0}) at {WIDTH}x{HEIGHT}, full frames"
+    step = frames_idx[1] - frames_idx[0] if len(frames_idx) > 1 else 0
+    desc = (f"{len(sample)} of {len(scenes)} fly-through frames ({frames_idx[0]}..{frames_idx[-1]} step {step}) "
+            f"at {WIDTH}x{HEIGHT}, full frames")
     try:
         if not refbridge.available():
             raise RuntimeError("reference runner unavailable")
-        # the reference renders its own scene type: planar disc mapping is its
-        # only mapping; the geometry and ray count are the workload's
         _, timing = refbridge.render(sample, threads=threads, timed=True)
         return timing["mrays_per_s"], timing["threads"], "reference", desc
-    except Exception as exc:  # fall back to the restatement
+    except Exception as exc:  # the restatement of the same loop
         print(f"# reference runner not used: {exc}", file=sys.stderr)
         t0 = time.perf_counter()
         for sc in sample:
             oracle.render_ref(sc, threads=threads)
         dt = time.perf_counter() - t0
-        rays = len(sample) * WIDTH * HEIGHT
-        return rays / dt / 1e6, threads or oracle.max_threads(), "port", desc
+        return len(sample) * WIDTH * HEIGHT / dt / 1e6, threads or oracle.max_threads(), "port", desc
 
 
 def run_reference(args):
-    rank, world, _ = dist_env()
+    rank, _, _ = dist_env()
     if rank != 0:
         return 0
     from blackhole_8_gb300 import scene as S
@@ -149,9 +145,7 @@ def run_reference(args):
     sample = [0, 40, 80, 119]
     for _ in range(args.warmup):
         cpu_reference(scenes, sample, threads)
-    vals = []
-    kind = desc = None
-    used = threads
+    vals, kind, desc, used = [], None, None, threads
     t_all = time.perf_counter()
     for _ in range(args.steps):
         v, used, kind, desc = cpu_reference(scenes, sample, threads)
@@ -159,22 +153,18 @@ def run_reference(args):
     wall = time.perf_counter() - t_all
     value = sum(vals) / len(vals)
     rays_step = len(sample) * WIDTH * HEIGHT
-    line = {
+    print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(rays_step / (value * 1e6) * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample_per_step": desc, "integrator": "reference trapezoid 20+20"},
-        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": used, "kind": kind,
-                         "sample": desc},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": used, "kind": kind, "sample": desc},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": round(wall, 2),
-    }
-    print(json.dumps(line))
+        "wall_s": round(wall, 2)}))
     return 0
 
 
-# ---------------------------------------------------------------------------
 def run_ours(args):
     rank, world, local = dist_env()
     import torch
@@ -196,9 +186,7 @@ def run_ours(args):
     px = torch.empty((FRAMES, HEIGHT, WIDTH, 4), dtype=torch.uint8, device="cuda")
     frames = (capi.Frame * FRAMES)()
     for i in range(FRAMES):
-        frames[i].pixels = px[i].data_ptr()
-        frames[i].hit_class = None
-        frames[i].aux = None
+        frames[i] = capi.Frame(px[i].data_ptr(), None, None)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     def barrier():
@@ -206,7 +194,18 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def time_sequence(opts, launches_per_step):
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    launches = 0
+
+    def time_sequence(opts, kernels_per_step):
+        nonlocal launches
         seq = r.sequence(cs, frames, opts)
         for _ in range(args.warmup):
             seq.launch()
@@ -226,66 +225,74 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier()
         wall = time.perf_counter() - t0
-        ms = [a.elapsed_time(b) for a, b in evs]
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
         st = seq.stats()
         seq.close()
-        return sum(ms) / len(ms), st, wall, launches_per_step * args.steps
-
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        launches += kernels_per_step * args.steps
+        return max_over_ranks(ms), st, wall
 
     fp32_tflops, sm_count = r.fp32_peak()
     fp64_tflops = r.fp64_peak()
 
-    clocks = ClockSampler(local)
-    clocks.start()
-    mixed_opts = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
-    plain_opts = capi.default_options(precision=capi.PRECISION_FP32, schedule=capi.SCHEDULE_GRID)
-    ms_mixed, st_mixed, wall_mixed, launches_mixed = time_sequence(mixed_opts, 2)
-    ms_plain, st_plain, wall_plain, launches_plain = time_sequence(plain_opts, 1)
-    clock_info = clocks.stop()
+    # autotuner (outside the timed region)
+    t0 = time.perf_counter()
+    tuned, rep = r.autotune(cs, capi.default_options(), max_error=MAX_DEFLECTION_ERROR)
+    tune_s = time.perf_counter() - t0
 
     rays_step = FRAMES * WIDTH * HEIGHT
-    ms_mixed_max = max_over_ranks(ms_mixed)
-    ms_plain_max = max_over_ranks(ms_plain)
-    value = rays_step * world / (ms_mixed_max * 1e-3) / 1e6
-    plain_value = rays_step * world / (ms_plain_max * 1e-3) / 1e6
+    variants = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_tuned, st_tuned, wall_tuned = time_sequence(tuned, 2)
+    eq = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
+    for name, opts, k in [
+        ("mixed_batched_step0.01", eq, 2),
+        ("plain_fp32_grid", capi.default_options(precision=capi.PRECISION_FP32), 1),
+        ("plain_fp32_persistent", capi.default_options(precision=capi.PRECISION_FP32,
+                                                       schedule=capi.SCHEDULE_PERSISTENT), 1),
+    ]:
+        ms, st, wall = time_sequence(opts, k)
+        fp32_steps = st.steps - st.band_steps
+        variants[name] = {"mrays_per_s": round(rays_step * world / (ms * 1e-3) / 1e6, 3),
+                          "ms_per_step": round(ms, 3), "step": opts.step, "steps_total": int(st.steps),
+                          "band_rays": int(st.band_rays),
+                          "fp32_tflops": round(fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms * 1e-3) / 1e12, 3),
+                          "wall_s": round(wall, 3)}
+    clock_info = clocks.stop()
 
-    # roofline: algorithmic FP32 flops of the RK4 steps of the dominant (FP32)
-    # pass per launch over the launch's device time
-    fp32_steps = st_mixed.steps - st_mixed.band_steps
-    achieved = fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms_mixed * 1e-3) / 1e12
-    plain_achieved = st_plain.steps * capi.RK4_FLOPS_PER_STEP / (ms_plain * 1e-3) / 1e12
+    value = rays_step * world / (ms_tuned * 1e-3) / 1e6
+    fp32_steps = st_tuned.steps - st_tuned.band_steps
+    achieved = fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms_tuned * 1e-3) / 1e12
+    issue_frac = fp32_steps * capi.RK4_INSTRUCTIONS_PER_STEP / (ms_tuned * 1e-3) / (fp32_tflops * 1e12 / 2)
+    variants["mixed_batched_tuned"] = {
+        "mrays_per_s": round(value, 3), "ms_per_step": round(ms_tuned, 3), "step": tuned.step,
+        "band": tuned.band, "threads_per_block": tuned.threads_per_block,
+        "refill_threshold": tuned.refill_threshold, "slice_steps": tuned.slice_steps,
+        "steps_total": int(st_tuned.steps), "band_rays": int(st_tuned.band_rays),
+        "band_fraction": st_tuned.band_rays / rays_step, "band_steps": int(st_tuned.band_steps),
+        "wall_s": round(wall_tuned, 3)}
 
-    # end to end through bh_render with host buffers
     e2e = None
     if not args.no_e2e:
         host = torch.empty((FRAMES, HEIGHT, WIDTH, 3), dtype=torch.uint8, pin_memory=True)
         hframes = (capi.Frame * FRAMES)()
         for i in range(FRAMES):
-            hframes[i].pixels = host[i].data_ptr()
-            hframes[i].hit_class = None
-            hframes[i].aux = None
-        e2e_opts = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
-                                        format=capi.FORMAT_BGR8)
+            hframes[i] = capi.Frame(host[i].data_ptr(), None, None)
+        e2e_opts = capi.RenderOptions()
+        import ctypes
+        ctypes.memmove(ctypes.byref(e2e_opts), ctypes.byref(tuned), ctypes.sizeof(e2e_opts))
+        e2e_opts.format = capi.FORMAT_BGR8
         for _ in range(max(1, args.warmup)):
             r.render_into(cs, hframes, e2e_opts)
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             r.render_into(cs, hframes, e2e_opts)
-        dt = (time.perf_counter() - t0) / args.steps
-        dt = max_over_ranks(dt)
+        dt = max_over_ranks((time.perf_counter() - t0) / args.steps)
         st_e2e = r.stats()
         e2e = {"value": round(rays_step * world / dt / 1e6, 3), "unit": "Mrays/s",
-               "h2d_bytes_per_step": int(st_e2e.h2d_bytes),
-               "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
-               "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)"}
+               "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
+               "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)", "call": "bh_render"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -293,38 +300,28 @@ def run_ours(args):
         cpu = {"value": round(v, 4), "unit": "Mrays/s", "cores": used, "kind": kind, "sample": desc}
 
     if rank == 0:
-        line = {
+        print(json.dumps({
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_mixed_max, 3),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_tuned, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": WORKLOAD, "tracer": "mixed-precision batched (persistent, FP64 band "
-                                                       f"|b-b_c|<{mixed_opts.band} M)",
-                       "frames": FRAMES, "width": WIDTH, "height": HEIGHT,
+            "data": "synthetic (seeded hash textures, procedural camera spiral)",
+            "config": {"workload": WORKLOAD, "frames": FRAMES, "width": WIDTH, "height": HEIGHT,
+                       "tracer": "mixed-precision batched, autotuned", "max_deflection_error_rad": MAX_DEFLECTION_ERROR,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
-            "variants": {
-                "mixed_batched": {"mrays_per_s": round(value, 3), "ms_per_step": round(ms_mixed_max, 3),
-                                  "steps_total": int(st_mixed.steps), "band_rays": int(st_mixed.band_rays),
-                                  "band_fraction": st_mixed.band_rays / rays_step,
-                                  "band_steps": int(st_mixed.band_steps), "band_overflow": int(st_mixed.band_overflow),
-                                  "wall_s": round(wall_mixed, 3)},
-                "plain_fp32": {"mrays_per_s": round(plain_value, 3), "ms_per_step": round(ms_plain_max, 3),
-                               "steps_total": int(st_plain.steps),
-                               "fp32_tflops": round(plain_achieved, 3),
-                               "frac_of_fp32_peak": round(plain_achieved / fp32_tflops, 4),
-                               "wall_s": round(wall_plain, 3)},
-            },
+            "accuracy": {"max_deflection_rad": rep.max_deflection, "max_hit_radius_error_M": rep.max_radius_error,
+                         "class_mismatch": rep.class_mismatch,
+                         "vs": "FP64 render (RK4, step 0.01) of frames 0/39/79/119; that path matches the CPU "
+                               "FP64 oracle in tests"},
+            "autotune": {"step": tuned.step, "candidates": rep.candidates, "seconds": round(tune_s, 2)},
+            "variants": variants,
             "roofline": {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_tflops, 3),
                          "unit": "TFLOP/s", "frac": round(achieved / fp32_tflops, 4), "traffic": None,
+                         "fp32_issue_frac": round(issue_frac, 4),
                          "peak_source": "measured in this run: FMA microbenchmark bh_probe_fp32_peak",
-                         "flops_per_step": capi.RK4_FLOPS_PER_STEP, "sm_count": sm_count,
+                         "flops_per_step": capi.RK4_FLOPS_PER_STEP,
+                         "instructions_per_step": capi.RK4_INSTRUCTIONS_PER_STEP, "sm_count": sm_count,
                          "fp64_peak_tflops_measured": round(fp64_tflops, 3)},
-            "clocks": clock_info,
-            "e2e": e2e,
-            "gpu_launches": launches_mixed + launches_plain,
-            "cpu_baseline": cpu,
-        }
-        print(json.dumps(line))
+            "clocks": clock_info, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu}))
     r.close()
     if world > 1:
         import torch.distributed as dist
@@ -334,9 +331,7 @@ def run_ours(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
-        return run_reference(args)
-    return run_ours(args)
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
 
 
 if __name__ == "__main__":

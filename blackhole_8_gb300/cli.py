@@ -56,6 +56,7 @@ def main(argv=None) -> int:
     ap.add_argument("--setup-band", type=float, default=-1)
     ap.add_argument("--slice", type=int, default=0)
     ap.add_argument("--refill", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ppm", default="")
     args = ap.parse_args(argv)
@@ -71,7 +72,7 @@ def main(argv=None) -> int:
     opts = capi.default_options(integrator=INTEGRATORS[args.integrator], precision=PRECISIONS[args.precision],
                                 schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
                                 band=args.band, setup_band=args.setup_band, slice_steps=args.slice,
-                                refill_threshold=args.refill)
+                                refill_threshold=args.refill, threads_per_block=args.threads)
     with Renderer(0) as r:
         cs = r.c_scenes(scenes)
         import torch

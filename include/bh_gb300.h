@@ -292,7 +292,9 @@ int bh_probe_fp32_peak(bh_ctx* ctx, double* tflops, int32_t* sm_count);
 int bh_probe_fp64_peak(bh_ctx* ctx, double* tflops);
 
 /* Algorithmic FP32 flops of one RK4 step of the tracer (FMA = 2). */
-#define BH_RK4_FLOPS_PER_STEP 36
+#define BH_RK4_FLOPS_PER_STEP 28
+/* FP32 instructions of one RK4 step (Runge-Kutta-Nystrom form). */
+#define BH_RK4_INSTRUCTIONS_PER_STEP 18
 
 #ifdef __cplusplus
 }
