@@ -16,6 +16,9 @@ A step is one pass of the tracer over the whole fly-through (120 frames of
   pinned host memory inside the timed region.
 - ``cpu_baseline``: the reference's own render loop (oracle/_ref, its
   20+20-step trapezoid scheme, FP64) on all host cores, on 8 of the 120 frames.
+- ``adjoint``: bh_render_adjoint on the 512x512 inverse-render workload
+  (forward + reverse pass per ray, Mrays/s) in MIXED, FP64 and FP32, with
+  each gradient's error against the FP64 one.
 
 ``--impl reference`` times only that reference CPU render (rank 0).
 Multi-GPU: every rank renders its own copy of the fly-through (replicas, no
@@ -50,6 +53,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     return ap.parse_args()
 
 
@@ -163,6 +167,64 @@ def run_reference(args):
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": round(wall, 2)}))
     return 0
+
+
+ADJ_SIDE = 512
+ADJ_WORKLOAD = "adjoint 512x512: MSE vs target at M+5%, disc tilt +3 deg, r_out +2M, yaw/pitch +1 deg; " \
+               "gradient w.r.t. M, camera position and yaw/pitch/roll, disc tilt, r_in, r_out; checkpoints every 64 steps"
+
+
+def adjoint_leg(r, args):
+    """Times bh_render_adjoint on the 512x512 inverse-render workload (the
+    target rendered by the library's FP64 forward at the perturbed theta)."""
+    import math
+
+    import numpy as np
+    import torch
+
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+
+    sc = S.single_scene(ADJ_SIDE, ADJ_SIDE)
+    th0 = np.array([sc.hole.mass(), 0, 0, 0, 0, 0, 0, 0, sc.disc.r_inner(), sc.disc.r_outer()], dtype=np.float64)
+    tt = th0.copy()
+    tt[capi.GRAD_MASS] *= 1.05
+    tt[capi.GRAD_TILT] += math.radians(3)
+    tt[capi.GRAD_R_OUTER] += 2.0
+    tt[capi.GRAD_YAW] += math.radians(1)
+    tt[capi.GRAD_PITCH] += math.radians(1)
+    cs = r.c_scenes([sc])
+    target = torch.zeros((ADJ_SIDE, ADJ_SIDE, 3), dtype=torch.float32, device="cuda")
+    fr = (capi.AdjointFrame * 1)()
+    fr[0].image = target.data_ptr()
+    r.render_adjoint(cs, fr, tt[None], capi.adjoint_options(precision=capi.PRECISION_FP64))
+    fr = (capi.AdjointFrame * 1)()
+    fr[0].target = target.data_ptr()
+    rays = ADJ_SIDE * ADJ_SIDE
+    out = {}
+    for name, prec in (("mixed", capi.PRECISION_MIXED), ("fp64", capi.PRECISION_FP64),
+                       ("fp32", capi.PRECISION_FP32)):
+        opts = capi.adjoint_options(precision=prec)
+        for _ in range(args.warmup):
+            r.render_adjoint(cs, fr, th0[None], opts)
+        ms = []
+        for _ in range(args.steps):
+            res = r.render_adjoint(cs, fr, th0[None], opts)[0]
+            ms.append(res.kernel_ms)
+        best = sum(ms) / len(ms)
+        out[name] = {"mrays_per_s": round(rays / (best * 1e-3) / 1e6, 3), "ms": round(best, 3),
+                     "loss": res.loss, "grad": [float(g) for g in res.grad], "steps": int(res.steps),
+                     "band_rays": int(res.band_rays), "band": opts.band if prec == capi.PRECISION_MIXED else None}
+    g64 = np.array(out["fp64"]["grad"])
+    for name in ("mixed", "fp32"):
+        g = np.array(out[name]["grad"])
+        out[name]["grad_rel_error_vs_fp64"] = float(np.linalg.norm(g - g64) / np.linalg.norm(g64))
+        out[name]["max_component_rel_error_vs_fp64"] = float(np.max(np.abs(g - g64) / np.abs(g64)))
+    return {"workload": ADJ_WORKLOAD, "metric": "adjoint Mrays/s (forward + reverse, per ray)",
+            "value": out["mixed"]["mrays_per_s"], "precision": "mixed (default)", "grad_names": list(capi.GRAD_NAMES),
+            "variants": out,
+            "verification": "tests/test_gpu_adjoint.py: FP64 adjoint vs FP64 dual numbers per pixel and vs "
+                            "FP64 central differences (h=1e-5) per parameter to 1e-3"}
 
 
 def run_ours(args):
@@ -294,6 +356,10 @@ def run_ours(args):
                "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
                "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)", "call": "bh_render"}
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_leg(r, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, used, kind, desc = cpu_reference(scenes, CPU_SAMPLE_FRAMES, os.cpu_count() or 1)
@@ -321,7 +387,8 @@ def run_ours(args):
                          "flops_per_step": capi.RK4_FLOPS_PER_STEP,
                          "instructions_per_step": capi.RK4_INSTRUCTIONS_PER_STEP, "sm_count": sm_count,
                          "fp64_peak_tflops_measured": round(fp64_tflops, 3)},
-            "clocks": clock_info, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu}))
+            "clocks": clock_info, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
+            "adjoint": adjoint}))
     r.close()
     if world > 1:
         import torch.distributed as dist

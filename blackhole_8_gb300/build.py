@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(PKG, "_lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libbh_gb300.so")
 
-SOURCES = ["bh_kernels.cu", "bh_capi.cu", "bh_noalloc.cu"]
+SOURCES = ["bh_kernels.cu", "bh_capi.cu", "bh_noalloc.cu", "bh_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]

@@ -157,3 +157,41 @@ class TuneReport(C.Structure):
 
 SIGNATURES["bh_autotune"] = (C.c_int, [C.c_void_p, C.POINTER(Scene), C.c_int32, C.POINTER(RenderOptions),
                                        C.c_double, C.c_char_p, C.POINTER(TuneReport)])
+
+# differentiable render and its adjoint
+GRAD_MASS, GRAD_CAM_X, GRAD_CAM_Y, GRAD_CAM_Z, GRAD_YAW, GRAD_PITCH, GRAD_ROLL, GRAD_TILT, GRAD_R_INNER, \
+    GRAD_R_OUTER = range(10)
+GRAD_COUNT = 10
+GRAD_NAMES = ("mass", "cam_x", "cam_y", "cam_z", "yaw", "pitch", "roll", "tilt", "r_inner", "r_outer")
+
+
+class AdjointOptions(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int32), ("step", C.c_double),
+                ("r_escape", C.c_double), ("softness", C.c_double), ("band", C.c_double),
+                ("checkpoint_every", C.c_int32), ("threads_per_block", C.c_int32), ("reserved", C.c_int32 * 8)]
+
+
+class AdjointFrame(C.Structure):
+    _fields_ = [("target", C.c_void_p), ("image", C.c_void_p), ("pixel_grad", C.c_void_p)]
+
+
+class AdjointResult(C.Structure):
+    _fields_ = [("loss", C.c_double), ("grad", C.c_double * GRAD_COUNT), ("steps", C.c_uint64),
+                ("band_rays", C.c_uint64), ("kernel_ms", C.c_double)]
+
+
+SIGNATURES["bh_adjoint_default_options"] = (None, [C.POINTER(AdjointOptions)])
+SIGNATURES["bh_render_adjoint"] = (C.c_int, [C.c_void_p, C.POINTER(Scene), C.c_int32, C.c_void_p,
+                                             C.POINTER(AdjointFrame), C.POINTER(AdjointOptions),
+                                             C.POINTER(AdjointResult)])
+SIGNATURES["bh_scene_at_theta"] = (C.c_int, [C.POINTER(Scene), C.c_void_p, C.POINTER(Scene)])
+
+
+def adjoint_options(**overrides) -> AdjointOptions:
+    o = AdjointOptions()
+    load().bh_adjoint_default_options(C.byref(o))
+    for k, v in overrides.items():
+        if not hasattr(o, k):
+            raise AttributeError(f"no adjoint option {k!r}")
+        setattr(o, k, v)
+    return o

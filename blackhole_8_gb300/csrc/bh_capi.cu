@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "bh_adjoint.h"
 #include "bh_internal.h"
 
 using bhgb::DevCounters;
@@ -62,6 +63,14 @@ struct bh_ctx {
   bool stats_valid = false;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   bh_render_stats last{};
+  // differentiable render
+  PinnedBuf<bhgb::adj::AdjScene> h_adj;
+  DevBuf<bhgb::adj::AdjScene> d_adj;
+  DevBuf<uint8_t> adj_ckpt, adj_ckpt_band;
+  DevBuf<uint2> adj_band;
+  DevBuf<double> adj_acc;
+  PinnedBuf<double> h_adj_acc;
+  DevBuf<unsigned long long> adj_counters;
 };
 
 struct bh_sequence {
@@ -513,6 +522,14 @@ void bh_destroy(bh_ctx* ctx) {
   if (ctx->out_arena.ptr) cudaFree(ctx->out_arena.ptr);
   if (ctx->d_counters) cudaFree(ctx->d_counters);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->h_adj.ptr) cudaFreeHost(ctx->h_adj.ptr);
+  if (ctx->d_adj.ptr) cudaFree(ctx->d_adj.ptr);
+  if (ctx->adj_ckpt.ptr) cudaFree(ctx->adj_ckpt.ptr);
+  if (ctx->adj_ckpt_band.ptr) cudaFree(ctx->adj_ckpt_band.ptr);
+  if (ctx->adj_band.ptr) cudaFree(ctx->adj_band.ptr);
+  if (ctx->adj_acc.ptr) cudaFree(ctx->adj_acc.ptr);
+  if (ctx->h_adj_acc.ptr) cudaFreeHost(ctx->h_adj_acc.ptr);
+  if (ctx->adj_counters.ptr) cudaFree(ctx->adj_counters.ptr);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   if (ctx->ev_staged) cudaEventDestroy(ctx->ev_staged);
@@ -1099,6 +1116,242 @@ int bh_probe_fp64_peak(bh_ctx* ctx, double* tflops) {
   }
   cudaFree(sink);
   *tflops = best;
+  return BH_OK;
+}
+
+}  // extern "C"
+
+// ---- differentiable render and its adjoint ----------------------------------------
+namespace {
+
+bool finite_n(const double* v, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+// Rodrigues rotation of v about the unit axis a by th (FP64, in place).
+void rotate3(double* v, const double* a, double th) {
+  const double c = std::cos(th), s = std::sin(th);
+  const double k = dot3(a, v) * (1 - c);
+  const double x[3] = {a[1] * v[2] - a[2] * v[1], a[2] * v[0] - a[0] * v[2], a[0] * v[1] - a[1] * v[0]};
+  for (int i = 0; i < 3; ++i) v[i] = v[i] * c + x[i] * s + a[i] * k;
+}
+
+int scene_at_theta(const bh_scene& in, const double* th, bh_scene* out) {
+  bh_scene s = in;
+  const bh_camera& c0 = in.camera;
+  auto rot = [&](double* v) {
+    rotate3(v, c0.axis_x, th[BH_GRAD_ROLL]);
+    rotate3(v, c0.axis_y, th[BH_GRAD_PITCH]);
+    rotate3(v, c0.axis_z, th[BH_GRAD_YAW]);
+  };
+  rot(s.camera.axis_x);
+  rot(s.camera.axis_y);
+  rot(s.camera.axis_z);
+  for (int i = 0; i < 3; ++i) s.camera.position[i] += th[BH_GRAD_CAM_X + i];
+  s.hole.mass = th[BH_GRAD_MASS];
+  bh_disc& d = s.disc;
+  const double l1 = std::sqrt(dot3(in.disc.edge_s1, in.disc.edge_s1));
+  if (l1 > 0) {
+    const double e1[3] = {in.disc.edge_s1[0] / l1, in.disc.edge_s1[1] / l1, in.disc.edge_s1[2] / l1};
+    // tilt about e1 through the centre; the bounding quad follows r_outer
+    const double scale = in.disc.r_outer > 0 ? th[BH_GRAD_R_OUTER] / in.disc.r_outer : 1.0;
+    double corner[3];
+    for (int i = 0; i < 3; ++i) corner[i] = (in.disc.corner[i] - in.disc.center[i]) * scale;
+    rotate3(corner, e1, th[BH_GRAD_TILT]);
+    for (int i = 0; i < 3; ++i) {
+      d.corner[i] = in.disc.center[i] + corner[i];
+      d.edge_s1[i] = in.disc.edge_s1[i] * scale;
+      d.edge_s2[i] = in.disc.edge_s2[i] * scale;
+    }
+    rotate3(d.edge_s1, e1, th[BH_GRAD_TILT]);
+    rotate3(d.edge_s2, e1, th[BH_GRAD_TILT]);
+    rotate3(d.normal, e1, th[BH_GRAD_TILT]);
+  }
+  d.r_inner = th[BH_GRAD_R_INNER];
+  d.r_outer = th[BH_GRAD_R_OUTER];
+  *out = s;
+  return BH_OK;
+}
+
+int validate_adjoint_options(bh_ctx* ctx, const bh_adjoint_options& o) {
+  if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
+  if (!(o.step > 0 && o.step <= 0.3)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "step must be in (0, 0.3]");
+  if (o.max_steps < 1 || o.max_steps > 1000000)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e6]");
+  if (!(o.r_escape > 2.0) || !std::isfinite(o.r_escape))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "r_escape must exceed the horizon (2 M)");
+  if (!(o.softness > 0) || !std::isfinite(o.softness))
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "softness must be positive");
+  if (!(o.band >= 0) || !std::isfinite(o.band)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band must be >= 0");
+  if (o.checkpoint_every != bhgb::adj::kSeg)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "checkpoint_every must be %d", bhgb::adj::kSeg);
+  if (o.threads_per_block != bhgb::adj::kAdjThreads)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "threads_per_block must be %d", bhgb::adj::kAdjThreads);
+  return BH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bh_adjoint_default_options(bh_adjoint_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = BH_PRECISION_MIXED;
+  o->max_steps = 4000;
+  o->step = 0.01;
+  o->r_escape = 100.0;
+  o->softness = 0.1;
+  o->band = 0.3;
+  o->checkpoint_every = bhgb::adj::kSeg;
+  o->threads_per_block = bhgb::adj::kAdjThreads;
+}
+
+int bh_scene_at_theta(const bh_scene* scene, const double* theta, bh_scene* out) {
+  if (!scene || !theta || !out) return BH_ERR_INVALID_ARGUMENT;
+  if (!finite_n(theta, BH_GRAD_COUNT)) return BH_ERR_INVALID_ARGUMENT;
+  return scene_at_theta(*scene, theta, out);
+}
+
+int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const double* theta,
+                      const bh_adjoint_frame* frames, const bh_adjoint_options* opts, bh_adjoint_result* results) {
+  using namespace bhgb::adj;
+  if (!ctx) return BH_ERR_INVALID_ARGUMENT;
+  if (!scenes || !frames || n < 1 || n > 65535)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "need 1..65535 scenes with frames");
+  bh_adjoint_options o;
+  bh_adjoint_default_options(&o);
+  if (opts) {
+    o = *opts;
+    if (o.max_steps == 0) o.max_steps = 4000;
+    if (o.step == 0) o.step = 0.01;
+    if (o.r_escape == 0) o.r_escape = 100.0;
+    if (o.softness == 0) o.softness = 0.1;
+    if (o.band < 0) o.band = 0.3;
+    if (o.checkpoint_every == 0) o.checkpoint_every = kSeg;
+    if (o.threads_per_block == 0) o.threads_per_block = kAdjThreads;
+  }
+  int rc = validate_adjoint_options(ctx, o);
+  if (rc) return rc;
+  bh_render_options ro;
+  bh_default_options(&ro);
+  ro.integrator = BH_INTEGRATOR_RK4;
+  ro.r_escape = o.r_escape;
+  BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((rc = ensure_pinned(ctx, ctx->h_adj, size_t(n)))) return rc;
+  int64_t total_blocks = 0, total_rays = 0;
+  for (int i = 0; i < n; ++i) {
+    double th[BH_GRAD_COUNT];
+    if (theta) {
+      std::memcpy(th, theta + (size_t)i * BH_GRAD_COUNT, sizeof(th));
+      if (!finite_n(th, BH_GRAD_COUNT))
+        return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: theta has a non-finite value", i);
+    } else {
+      base_theta(scenes[i], th);
+    }
+    bh_scene posed;
+    scene_at_theta(scenes[i], th, &posed);
+    if ((rc = validate_scene(ctx, posed, i, ro))) return rc;
+    if (posed.disc.enabled && posed.disc.mapping != BH_DISC_MAP_POLAR)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: the differentiable render maps the disc POLAR", i);
+    const double* hp = scenes[i].hole.position;
+    const double* dc = scenes[i].disc.center;
+    if (posed.disc.enabled &&
+        std::sqrt((dc[0] - hp[0]) * (dc[0] - hp[0]) + (dc[1] - hp[1]) * (dc[1] - hp[1]) +
+                  (dc[2] - hp[2]) * (dc[2] - hp[2])) > 1e-9 * std::max(1.0, posed.hole.mass))
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: the differentiable render needs the disc centred on the hole", i);
+    AdjScene* a = ctx->h_adj.ptr + i;
+    std::memset(a, 0, sizeof(*a));
+    build_adj_scene(scenes[i], th, o.softness, a);
+    a->disc_on = posed.disc.enabled ? 1 : 0;
+    if (a->disc_on) {
+      const TexEntry& t = ctx->textures[posed.disc.texture];
+      a->disc_tex = bhgb::DevTexture{t.texels, t.width, t.height};
+    }
+    a->has_bg = posed.background >= 0 ? 1 : 0;
+    if (a->has_bg) {
+      const TexEntry& t = ctx->textures[posed.background];
+      a->bg_tex = bhgb::DevTexture{t.texels, t.width, t.height};
+    }
+    a->scene = i;
+    a->block_begin = total_blocks;
+    a->target = frames[i].target;
+    a->image = frames[i].image;
+    a->pixel_grad = frames[i].pixel_grad;
+    const int64_t tiles = int64_t(a->tiles_x) * ((posed.camera.height + 3) / 4);
+    total_blocks += (tiles + 3) / 4;
+    total_rays += int64_t(posed.camera.width) * posed.camera.height;
+  }
+  int main_grid = 0, band_grid = 0;
+  BH_CUDA(ctx, plan_adjoint(o.precision, ctx->sm_count, total_blocks, &main_grid, &band_grid));
+  const int64_t nseg = (o.max_steps - 1) / kSeg + 1;
+  const bool any_target = [&] {
+    for (int i = 0; i < n; ++i)
+      if (frames[i].target) return true;
+    return false;
+  }();
+  AdjLaunch L{};
+  L.scenes = nullptr;
+  L.n_scenes = n;
+  L.precision = o.precision;
+  L.p.c32 = exact_rk4_consts_f32(o.step, 1.0 / o.r_escape, o.max_steps);
+  L.p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
+  L.p.inv_h32 = 1.0 / double(L.p.c32.h);
+  L.p.inv_h64 = 1.0 / o.step;
+  L.p.softness = o.softness;
+  L.p.band = o.band;
+  L.p.kmax = o.max_steps;
+  L.p.want_grad = any_target ? 1 : 0;
+  L.total_blocks = total_blocks;
+  L.ckpt_slots = int64_t(main_grid) * kAdjThreads;
+  L.band_slots = int64_t(band_grid) * kAdjThreads;
+  const size_t ck_bytes = any_target ? size_t(L.ckpt_slots) * nseg * checkpoint_bytes(o.precision) : 16;
+  const size_t ckb_bytes =
+      any_target && band_grid ? size_t(L.band_slots) * nseg * band_checkpoint_bytes() : 16;
+  if ((rc = ensure_dev(ctx, ctx->d_adj, size_t(n)))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->adj_ckpt, ck_bytes))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->adj_ckpt_band, ckb_bytes))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->adj_acc, size_t(n) * kAccStride))) return rc;
+  if ((rc = ensure_pinned(ctx, ctx->h_adj_acc, size_t(n) * kAccStride))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->adj_counters, size_t(kCounters)))) return rc;
+  const uint32_t band_cap =
+      o.precision == BH_PRECISION_MIXED ? uint32_t(std::min<int64_t>(total_rays, int64_t(1) << 30)) : 1u;
+  if ((rc = ensure_dev(ctx, ctx->adj_band, size_t(band_cap)))) return rc;
+  L.scenes = ctx->d_adj.ptr;
+  L.ckpt = ctx->adj_ckpt.ptr;
+  L.ckpt_band = ctx->adj_ckpt_band.ptr;
+  L.band_list = ctx->adj_band.ptr;
+  L.band_capacity = band_cap;
+  L.counters = ctx->adj_counters.ptr;
+  L.acc = ctx->adj_acc.ptr;
+  cudaStream_t st = ctx->stream;
+  BH_CUDA(ctx, cudaMemcpyAsync(ctx->d_adj.ptr, ctx->h_adj.ptr, sizeof(AdjScene) * n, cudaMemcpyHostToDevice, st));
+  BH_CUDA(ctx, cudaMemsetAsync(ctx->adj_acc.ptr, 0, sizeof(double) * n * kAccStride, st));
+  BH_CUDA(ctx, cudaMemsetAsync(ctx->adj_counters.ptr, 0, sizeof(unsigned long long) * kCounters, st));
+  BH_CUDA(ctx, cudaEventRecord(ctx->ev_start, st));
+  BH_CUDA(ctx, launch_adjoint(L, main_grid, band_grid, st));
+  BH_CUDA(ctx, cudaEventRecord(ctx->ev_stop, st));
+  BH_CUDA(ctx, cudaMemcpyAsync(ctx->h_adj_acc.ptr, ctx->adj_acc.ptr, sizeof(double) * n * kAccStride,
+                               cudaMemcpyDeviceToHost, st));
+  BH_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0;
+  BH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  if (results) {
+    for (int i = 0; i < n; ++i) {
+      const double* a = ctx->h_adj_acc.ptr + (size_t)i * kAccStride;
+      const double norm = 3.0 * double(scenes[i].camera.width) * double(scenes[i].camera.height);
+      bh_adjoint_result& r = results[i];
+      std::memset(&r, 0, sizeof(r));
+      r.loss = a[0] / norm;
+      for (int k = 0; k < BH_GRAD_COUNT; ++k) r.grad[k] = a[1 + k] / norm;
+      r.steps = uint64_t(a[kAccSteps] + 0.5);
+      r.band_rays = uint64_t(a[kAccBandRays] + 0.5);
+      r.kernel_ms = ms;
+    }
+  }
   return BH_OK;
 }
 

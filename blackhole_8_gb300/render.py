@@ -147,6 +147,30 @@ class Renderer:
         _check(self.lib, self.ctx, rc)
         return out, rep
 
+    # -- differentiable render -----------------------------------------------------------
+    def render_adjoint(self, c_scenes, frames, theta=None,
+                       options: capi.AdjointOptions | None = None) -> list[capi.AdjointResult]:
+        """bh_render_adjoint: ``frames`` is a ctypes array of AdjointFrame with
+        device pointers; ``theta`` an (n, 10) float64 array or None (each
+        scene's own parameters). Returns loss and gradient per scene."""
+        n = len(c_scenes)
+        res = (capi.AdjointResult * n)()
+        th = None
+        if theta is not None:
+            th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(n, capi.GRAD_COUNT))
+        opts = options or capi.adjoint_options()
+        rc = self.lib.bh_render_adjoint(self.ctx, c_scenes, n, th.ctypes.data if th is not None else None, frames,
+                                        C.byref(opts), res)
+        _check(self.lib, self.ctx, rc)
+        return list(res)
+
+    def scene_at_theta(self, c_scene: capi.Scene, theta) -> capi.Scene:
+        """The scene moved to theta (bh_scene_at_theta)."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(capi.GRAD_COUNT))
+        out = capi.Scene()
+        _check(self.lib, self.ctx, self.lib.bh_scene_at_theta(C.byref(c_scene), th.ctypes.data, C.byref(out)))
+        return out
+
     # -- probes ---------------------------------------------------------------------------
     def fp32_peak(self) -> tuple[float, int]:
         t = C.c_double()

@@ -285,6 +285,83 @@ int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, const bh_de
                       int32_t n_textures, const bh_frame* frames, const bh_render_options* opts, void* stream,
                       char* error, int32_t error_len);
 
+/* ---- differentiable render and its adjoint -------------------------------------
+ * No counterpart in the reference (it has no gradients and no smooth mode).
+ * A smooth variant of the RK4 render, so that an image loss has gradients:
+ *   - disc: bilinear texture in (radius, azimuth), texel x over [r_in, r_out]
+ *     (POLAR mapping about the hole), opacity
+ *     alpha = s((R - r_in)/w) s((r_out - R)/w), s the logistic function,
+ *     w = softness * M; crossings composite front to back
+ *     (C += T alpha C_disc, T *= 1 - alpha); the ray stops once T < 1e-4;
+ *   - sky: bilinear equirectangular background at the escape direction;
+ *   - horizon and step cap: black.
+ * Colours are linear RGB in [0, 1] (texel / 255), float32, H*W*3 row-major.
+ * The parameters theta (BH_GRAD_COUNT doubles per scene) are taken about the
+ * scene: M; camera position offset (x, y, z); camera yaw, pitch and roll,
+ * rotations of the camera axes about the scene camera's own axis_z, axis_y
+ * and axis_x, applied as R(z, yaw) R(y, pitch) R(x, roll); disc tilt, a
+ * rotation of the disc normal about the disc's in-plane axis edge_s1/|s1|;
+ * r_inner; r_outer. theta = NULL means the scene itself (M, zeros, its radii).
+ * bh_render_adjoint renders every scene at its theta and, for frames with a
+ * target, returns loss = mean over H*W*3 of (C - target)^2 and its gradient
+ * with respect to theta. The gradient is reverse mode through the fixed-step
+ * RK4 integrator with a checkpoint of the trajectory every
+ * checkpoint_every steps (recomputed in 8-step pieces on the way back).
+ * Buffers in `frames` are device memory; results are written to the host
+ * array `results` (may be NULL) when the call returns. Enqueued on the
+ * context's stream; the call waits for it. */
+enum {
+  BH_GRAD_MASS = 0,
+  BH_GRAD_CAM_X = 1,
+  BH_GRAD_CAM_Y = 2,
+  BH_GRAD_CAM_Z = 3,
+  BH_GRAD_YAW = 4,
+  BH_GRAD_PITCH = 5,
+  BH_GRAD_ROLL = 6,
+  BH_GRAD_TILT = 7,
+  BH_GRAD_R_INNER = 8,
+  BH_GRAD_R_OUTER = 9,
+  BH_GRAD_COUNT = 10
+};
+
+typedef struct bh_adjoint_options {
+  int32_t precision;         /* FP64; FP32 (plain FP32 throughout); MIXED (default):
+                                FP64 ray setup and crossing phases, FP32 integration
+                                with compensated state updates, and rays with
+                                |b/M - 3 sqrt 3| < band entirely in FP64 */
+  int32_t max_steps;         /* default 4000 */
+  double step;               /* RK4 step in phi, default 0.01 (at most 0.3) */
+  double r_escape;           /* escape radius in units of M, default 100 */
+  double softness;           /* disc-edge width in units of M, default 0.1 */
+  double band;               /* MIXED FP64 band in units of M, default 0.3 */
+  int32_t checkpoint_every;  /* steps between trajectory checkpoints: 64 */
+  int32_t threads_per_block; /* 0 = default (128, a multiple of 32 up to 256) */
+  int32_t reserved[8];
+} bh_adjoint_options;
+
+typedef struct bh_adjoint_frame {
+  const float* target;  /* device, H*W*3 RGB; NULL renders without gradient */
+  float* image;         /* device, H*W*3 RGB, or NULL */
+  float* pixel_grad;    /* device, H*W*BH_GRAD_COUNT, or NULL: per pixel the
+                           gradient of sum_c (C_c - target_c)^2 (not divided
+                           by H*W*3) */
+} bh_adjoint_frame;
+
+typedef struct bh_adjoint_result {
+  double loss;                 /* mean over H*W*3 of (C - target)^2 */
+  double grad[BH_GRAD_COUNT];  /* d loss / d theta */
+  uint64_t steps;              /* RK4 steps of the forward pass */
+  uint64_t band_rays;          /* MIXED: rays traced in FP64 */
+  double kernel_ms;            /* device time of the call's kernels (all scenes) */
+} bh_adjoint_result;
+
+void bh_adjoint_default_options(bh_adjoint_options* opts);
+int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const double* theta,
+                      const bh_adjoint_frame* frames, const bh_adjoint_options* opts, bh_adjoint_result* results);
+/* The scene moved to theta (pose, disc normal, M and radii replaced): what
+ * bh_render_adjoint renders for theta, as a scene for the other renders. */
+int bh_scene_at_theta(const bh_scene* scene, const double* theta, bh_scene* out);
+
 /* ---- device probes ------------------------------------------------------------
  * Measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops) and its
  * multiprocessor count; used as the roofline denominator. */

@@ -1,4 +1,6 @@
-"""Test infrastructure: builds and binds the FP64 CPU oracle (bh_oracle.c).
+"""Test infrastructure: builds and binds the FP64 CPU oracles (bh_oracle.c:
+the reference's trapezoid render and the RK4 render; bh_oracle_smooth.cc:
+the differentiable render, its forward-mode dual-number gradient).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` use this module, always as the checker, never as the product.
@@ -31,14 +33,22 @@ class OrcOutputs(C.Structure):
                 ("margin_r", C.c_void_p), ("b_over_m", C.c_void_p), ("steps", C.c_void_p)]
 
 
+SRC_SMOOTH = os.path.join(HERE, "bh_oracle_smooth.cc")
+
+
 def build(force: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(ROOT, "include", "bh_gb300.h"))):
+    inc = os.path.join(ROOT, "include")
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(SRC_SMOOTH), os.path.getmtime(os.path.join(inc, "bh_gb300.h")))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     os.makedirs(BUILD_DIR, exist_ok=True)
+    obj_c = os.path.join(BUILD_DIR, "bh_oracle.o")
+    obj_cc = os.path.join(BUILD_DIR, "bh_oracle_smooth.o")
+    subprocess.run(["gcc", "-O2", "-fopenmp", "-fPIC", "-std=c11", "-I", inc, "-c", SRC, "-o", obj_c], check=True)
+    subprocess.run(["g++", "-O2", "-fopenmp", "-fPIC", "-std=c++17", "-I", inc, "-c", SRC_SMOOTH, "-o", obj_cc],
+                   check=True)
     tmp = LIB + ".tmp"
-    subprocess.run(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-I", os.path.join(ROOT, "include"),
-                    SRC, "-o", tmp, "-lm"], check=True)
+    subprocess.run(["g++", "-shared", "-fopenmp", obj_c, obj_cc, "-o", tmp, "-lm"], check=True)
     os.replace(tmp, LIB)
     return LIB
 
@@ -136,3 +146,65 @@ def render_rk4(scene, step: float = 0.01, max_steps: int = 4000, r_escape: float
 
 def max_threads() -> int:
     return load().orc_max_threads()
+
+
+# ---------------------------------------------------------------------------
+# differentiable render (bh_oracle_smooth.cc)
+class OrcSmoothOpts(C.Structure):
+    _fields_ = [("step", C.c_double), ("max_steps", C.c_int32), ("r_escape", C.c_double), ("softness", C.c_double)]
+
+
+N_PARAMS = 10
+
+
+def _smooth_args(scene, step, max_steps, r_escape, softness, scene_c=None):
+    s = _scene_c(scene) if scene_c is None else scene_c
+    dtex = np.ascontiguousarray(scene.disc.texture.bgra())
+    bg = np.ascontiguousarray(scene.background.bgra()) if scene.background is not None else None
+    opts = OrcSmoothOpts(step, max_steps, r_escape, softness)
+    return s, dtex, bg, opts
+
+
+def base_theta(scene) -> np.ndarray:
+    """theta of a scene itself: M, zero pose offsets, zero tilt, its radii."""
+    return np.array([scene.hole.mass(), 0, 0, 0, 0, 0, 0, 0, scene.disc.r_inner(), scene.disc.r_outer()],
+                    dtype=np.float64)
+
+
+def smooth_render(scene, theta=None, target=None, step=0.01, max_steps=4000, r_escape=100.0, softness=0.1,
+                  threads=0, scene_c=None):
+    """Differentiable render at theta (FP64): image (H, W, 3), per-pixel loss
+    sum_c (C - target)^2, per-pixel ray signature. scene_c (a bh_scene)
+    replaces the poses of `scene`, whose textures are used."""
+    lib = load()
+    lib.orc_smooth_render.restype = C.c_int
+    s, dtex, bg, opts = _smooth_args(scene, step, max_steps, r_escape, softness, scene_c)
+    th = np.ascontiguousarray(base_theta(scene) if theta is None else theta, dtype=np.float64)
+    h, w = scene.camera.height(), scene.camera.width()
+    img = np.zeros((h, w, 3))
+    loss = np.zeros((h, w))
+    sig = np.zeros((h, w), np.uint32)
+    tg = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+    lib.orc_smooth_render(C.byref(s), th.ctypes.data_as(C.c_void_p), dtex.ctypes.data_as(C.c_void_p),
+                          dtex.shape[1], dtex.shape[0], bg.ctypes.data_as(C.c_void_p) if bg is not None else None,
+                          bg.shape[1] if bg is not None else 0, bg.shape[0] if bg is not None else 0, C.byref(opts),
+                          tg.ctypes.data_as(C.c_void_p) if tg is not None else None, img.ctypes.data_as(C.c_void_p),
+                          loss.ctypes.data_as(C.c_void_p), sig.ctypes.data_as(C.c_void_p), threads)
+    return img, loss, sig
+
+
+def smooth_grad(scene, target, theta=None, step=0.01, max_steps=4000, r_escape=100.0, softness=0.1, threads=0):
+    """Per-pixel gradient (H, W, 10) of sum_c (C - target)^2 by FP64 forward
+    mode (dual numbers)."""
+    lib = load()
+    lib.orc_smooth_grad.restype = C.c_int
+    s, dtex, bg, opts = _smooth_args(scene, step, max_steps, r_escape, softness)
+    th = np.ascontiguousarray(base_theta(scene) if theta is None else theta, dtype=np.float64)
+    h, w = scene.camera.height(), scene.camera.width()
+    g = np.zeros((h, w, N_PARAMS))
+    tg = np.ascontiguousarray(target, dtype=np.float32)
+    lib.orc_smooth_grad(C.byref(s), th.ctypes.data_as(C.c_void_p), dtex.ctypes.data_as(C.c_void_p),
+                        dtex.shape[1], dtex.shape[0], bg.ctypes.data_as(C.c_void_p) if bg is not None else None,
+                        bg.shape[1] if bg is not None else 0, bg.shape[0] if bg is not None else 0, C.byref(opts),
+                        tg.ctypes.data_as(C.c_void_p), g.ctypes.data_as(C.c_void_p), threads)
+    return g

@@ -73,3 +73,57 @@ def class_boundary_mask(cls: np.ndarray) -> np.ndarray:
     m[:, 1:] |= cls[:, 1:] != cls[:, :-1]
     m[:, :-1] |= cls[:, :-1] != cls[:, 1:]
     return m
+
+
+# ---------------------------------------------------------------------------
+# differentiable render (adjoint) cases
+def adjoint_thetas(scene: S.Scene):
+    """theta of the scene itself and the target theta of the adjoint workload:
+    M + 5 %, disc tilt + 3 deg, r_outer + 2 M, camera yaw and pitch + 1 deg."""
+    from oracle import oracle
+    th0 = oracle.base_theta(scene)
+    tt = th0.copy()
+    tt[capi.GRAD_MASS] *= 1.05
+    tt[capi.GRAD_TILT] += math.radians(3)
+    tt[capi.GRAD_R_OUTER] += 2.0
+    tt[capi.GRAD_YAW] += math.radians(1)
+    tt[capi.GRAD_PITCH] += math.radians(1)
+    return th0, tt
+
+
+def adjoint_case(width: int, height: int):
+    """(scene, theta0, theta_target, target image float32 (H, W, 3)) with the
+    target rendered by the FP64 oracle."""
+    from oracle import oracle
+    sc = S.single_scene(width, height)
+    th0, tt = adjoint_thetas(sc)
+    target, _, _ = oracle.smooth_render(sc, tt)
+    return sc, th0, tt, np.ascontiguousarray(target.astype(np.float32))
+
+
+def fd_protocol(loss_at, theta: np.ndarray, i: int, h: float = 1e-5, signature_at=None):
+    """Central differences of the per-pixel loss in parameter i at h, h/2 and
+    h/4. Returns (Richardson estimate from h and h/2, mask of the pixels where
+    the estimate is trusted): the three differences agree within 1 % of the
+    estimate, or within 1e-6 of the largest estimate (the loss is resolved
+    at h) and, when signature_at is given, the
+    ray's structure is the same at all six points."""
+    fds = []
+    mask = None
+    base_sig = signature_at(theta) if signature_at else None
+    for hh in (h, h / 2, h / 4):
+        tp = theta.copy()
+        tp[i] += hh
+        tm = theta.copy()
+        tm[i] -= hh
+        lp, lm = loss_at(tp), loss_at(tm)
+        fds.append((lp - lm) / (2 * hh))
+        if signature_at:
+            same = (signature_at(tp) == base_sig) & (signature_at(tm) == base_sig)
+            mask = same if mask is None else mask & same
+    rich = (4 * fds[1] - fds[0]) / 3
+    # tiny derivatives are resolved to rounding only; they weigh nothing
+    atol = 1e-6 * float(np.abs(rich).max())
+    ok = (np.abs(fds[0] - fds[1]) <= 1e-2 * np.abs(rich) + atol) & \
+         (np.abs(fds[1] - fds[2]) <= 1e-2 * np.abs(rich) + atol)
+    return rich, ok if mask is None else ok & mask
