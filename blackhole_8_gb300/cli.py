@@ -6,6 +6,11 @@ prints one JSON line of timings.
 
     python -m blackhole_8_gb300.cli --workload flythrough --frames 8 \
         --precision fp32 --schedule grid --repeat 3 [--ppm DIR]
+
+``--workload adjoint`` runs the differentiable render instead: a target is
+rendered (FP64) at M + 5 %, disc tilt + 3 deg, r_outer + 2 M, yaw and pitch
++ 1 deg, then bh_render_adjoint gives the loss and its gradient at the
+scene's own parameters (--precision fp32|fp64|mixed), --repeat times.
 """
 from __future__ import annotations
 
@@ -43,7 +48,8 @@ def write_ppm(path: str, bgra) -> None:
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--workload", default="flythrough", choices=["single", "flythrough", "batched", "photon-ring"])
+    ap.add_argument("--workload", default="flythrough",
+                    choices=["single", "flythrough", "batched", "photon-ring", "adjoint"])
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
@@ -68,6 +74,8 @@ def main(argv=None) -> int:
     from . import build, capi
     from .render import Renderer
     build.build()
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     scenes = build_scenes(args)
     opts = capi.default_options(integrator=INTEGRATORS[args.integrator], precision=PRECISIONS[args.precision],
                                 schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
@@ -96,6 +104,48 @@ def main(argv=None) -> int:
             os.makedirs(args.ppm, exist_ok=True)
             for i, b in enumerate(bufs):
                 write_ppm(os.path.join(args.ppm, f"frame_{i:04d}.ppm"), b.cpu().numpy())
+        print(json.dumps(out))
+    return 0
+
+
+def run_adjoint(args) -> int:
+    import math
+
+    import numpy as np
+    import torch
+
+    from . import capi
+    from . import scene as S
+    from .render import Renderer
+    sc = S.single_scene(args.width or 512, args.height or 512)
+    th0 = np.array([sc.hole.mass(), 0, 0, 0, 0, 0, 0, 0, sc.disc.r_inner(), sc.disc.r_outer()], dtype=np.float64)
+    tt = th0.copy()
+    tt[capi.GRAD_MASS] *= 1.05
+    tt[capi.GRAD_TILT] += math.radians(3)
+    tt[capi.GRAD_R_OUTER] += 2.0
+    tt[capi.GRAD_YAW] += math.radians(1)
+    tt[capi.GRAD_PITCH] += math.radians(1)
+    h, w = sc.camera.height(), sc.camera.width()
+    with Renderer(0) as r:
+        cs = r.c_scenes([sc])
+        target = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+        fr = (capi.AdjointFrame * 1)()
+        fr[0].image = target.data_ptr()
+        r.render_adjoint(cs, fr, tt[None], capi.adjoint_options(precision=capi.PRECISION_FP64, max_steps=args.max_steps,
+                                                                step=args.step))
+        fr = (capi.AdjointFrame * 1)()
+        fr[0].target = target.data_ptr()
+        opts = capi.adjoint_options(precision=PRECISIONS[args.precision], max_steps=args.max_steps, step=args.step)
+        if args.band >= 0:
+            opts.band = args.band
+        times = []
+        for _ in range(args.repeat):
+            res = r.render_adjoint(cs, fr, th0[None], opts)[0]
+            times.append(res.kernel_ms)
+        out = {"workload": "adjoint", "width": w, "height": h, "precision": args.precision, "kernel_ms": times,
+               "mrays_per_s": w * h / (min(times) * 1e-3) / 1e6, "loss": res.loss,
+               "grad": dict(zip(capi.GRAD_NAMES, list(res.grad))), "steps": int(res.steps),
+               "band_rays": int(res.band_rays)}
         print(json.dumps(out))
     return 0
 

@@ -89,6 +89,7 @@ struct AdjScene {
   DevTexture disc_tex, bg_tex;
   int32_t width, height, tiles_x, disc_on, has_bg, scene;
   int64_t block_begin;  // first block of this scene in the grid
+  int64_t ray_begin;    // first ray of this scene (row-major pixels, scenes back to back)
   const float* target;
   float* image;
   float* pixel_grad;
@@ -99,6 +100,9 @@ struct AdjParams {
   Rk4Consts<double> c64;
   double inv_h32;    // 1 / step as the FP32 and FP64 integrations take it
   double inv_h64;
+  double hstep32;    // the step the FP32 / FP64 trajectories take (phases)
+  double hstep64;
+  float df_c[2 * 8]; // double-float split (hi, lo) of c64: h, hh, q, q2, h26, h6, x_esc, x_hor
   double softness;
   double band;       // MIXED: |b/M - 3 sqrt 3| < band goes to FP64
   int32_t kmax;
@@ -217,12 +221,36 @@ struct Traj {
 };
 
 // 2Sum (Knuth): s + e == a + b exactly.
+#if !defined(__CUDA_ARCH__)
+template <typename R>
+inline R rn_round(volatile R v) { return v; }
+template <typename R>
+BHA_HD R rn_add(R a, R b) { return rn_round<R>(a + b); }
+template <typename R>
+BHA_HD R rn_sub(R a, R b) { return rn_round<R>(a - b); }
+#else
+template <typename R>
+BHA_HD R rn_add(R a, R b) { return a + b; }
+template <typename R>
+BHA_HD R rn_sub(R a, R b) { return a - b; }
+#endif
+#if defined(__CUDA_ARCH__)
+template <>
+BHA_HD float rn_add<float>(float a, float b) { return __fadd_rn(a, b); }
+template <>
+BHA_HD float rn_sub<float>(float a, float b) { return __fsub_rn(a, b); }
+template <>
+BHA_HD double rn_add<double>(double a, double b) { return __dadd_rn(a, b); }
+template <>
+BHA_HD double rn_sub<double>(double a, double b) { return __dsub_rn(a, b); }
+#endif
+// (rounded separately: a product fused into these sums would break them)
 template <typename R>
 BHA_HD void two_sum_acc(R& a, R b, R& e) {
-  const R y = b + e;
-  const R s = a + y;
-  const R bb = s - a;
-  e = (a - (s - bb)) + (y - bb);
+  const R y = rn_add(b, e);
+  const R s = rn_add(a, y);
+  const R bb = rn_sub(s, a);
+  e = rn_add(rn_sub(a, rn_sub(s, bb)), rn_sub(y, bb));
   a = s;
 }
 
@@ -291,6 +319,32 @@ BHA_HD void step_vjp(R x, R w, const Rk4Consts<R>& c, R& lx, R& lw) {
   const R nlw = fma(c.h, s3ab, fma(c.hh, x2b, lw));
   lx = nlx;
   lw = nlw;
+}
+
+// step_vjp with the update of the adjoint written as lambda + delta and
+// accumulated with 2Sum (compensation terms clx, clw): the reverse pass of a
+// near-critical ray crosses the same unstable saddle as the forward pass, so
+// plain FP32 accumulation of lambda loses ~1e-3 there.
+template <typename R>
+BHA_HD void step_vjp_comp(R x, R w, const Rk4Consts<R>& c, R& lx, R& lw, R& clx, R& clw) {
+  const R a1 = fx(x);
+  const R x2 = fma(c.hh, w, x);
+  const R a2 = fx(x2);
+  const R x3 = fma(c.q, a1, x2);
+  const R s3a = fma(c.h, w, x);
+  const R x4 = fma(c.q2, a2, s3a);
+  const R S3b = c.h26 * lx;
+  const R S4b = c.h6 * lw;
+  const R a3b = fma(R(2), S4b, S3b);
+  const R x4b = S4b * dfx(x4);
+  const R a2b = fma(c.q2, x4b, a3b);
+  const R x3b = a3b * dfx(x3);
+  const R a1b = fma(c.q, x3b, S3b + S4b);
+  const R x2b = fma(a2b, dfx(x2), x3b);
+  const R dlx = fma(a1b, dfx(x), x4b + x2b);
+  const R dlw = fma(c.h, lx + x4b, c.hh * x2b);
+  two_sum_acc(lx, dlx, clx);
+  two_sum_acc(lw, dlw, clw);
 }
 
 // The same for a step of length h, with the adjoint of h.
@@ -443,6 +497,7 @@ struct Fwd {
   R trans;   // transmittance at the end
   R xa, wa, xb, wb;  // MISS: the states around the escape
   int32_t cls, k_end;
+  int32_t m_end;     // disc-plane crossing phases reached (DISC: index of the last)
 };
 
 // adjoints collected by the backward pass
@@ -486,6 +541,9 @@ BHA_HD int crossing_step(P dm, const AdjParams& p) {
   return int(floor(dm * P(sizeof(R) == sizeof(float) ? p.inv_h32 : p.inv_h64)));
 }
 
+template <typename R>
+BHA_HD double phase_step(const AdjParams& p) { return sizeof(R) == sizeof(float) ? p.hstep32 : p.hstep64; }
+
 template <typename P>
 BHA_HD P reduce_2pi(P a) { return a - P(kTwoPiD) * floor(a * P(1.0 / kTwoPiD)); }
 
@@ -509,7 +567,7 @@ BHA_HD bool crossing_eval(const AdjScene& s, const AdjParams& p, const RayC<R, P
                           Crossing<R, P>& c) {
   c.x = x;
   c.w = w;
-  c.delta = R(dm - P(kc) * P(consts<R>(p).h));
+  c.delta = R(dm - P(kc) * P(phase_step<R>(p)));
   R xc = x, wc = w;
   step_h(xc, wc, c.delta);
   c.uc = xc + R(1.0 / 3.0);
@@ -601,7 +659,7 @@ BHA_HD void escape_eval(const AdjScene& s, const AdjParams& p, const RayC<R, P>&
   e.t = t;
   e.hm = hermite(xa, c.h * wa, xb, c.h * wb, t);
   e.we = e.hm.dp / c.h;
-  const R psi = R(reduce_2pi(rc.phi0 + P(ka) * P(c.h))) + t * c.h + atan2(c.u_esc, -e.we);
+  const R psi = R(reduce_2pi(rc.phi0 + P(ka) * P(phase_step<R>(p)))) + t * c.h + atan2(c.u_esc, -e.we);
   e.psi_c = cos(psi);
   e.psi_s = sin(psi);
   e.dir = rc.yv * e.psi_c + rc.xv * e.psi_s;
@@ -616,9 +674,30 @@ BHA_HD void escape_eval(const AdjScene& s, const AdjParams& p, const RayC<R, P>&
 
 // ---------------------------------------------------------------------------
 // forward pass: colour, class and (want_grad) the checkpoints
-template <typename R, typename P, bool kComp>
+// Stored trajectory state of the FP64 band pass.
+template <typename R>
+struct Vec2T;
+template <>
+struct Vec2T<float> {
+  using type = float2;
+};
+template <>
+struct Vec2T<double> {
+  using type = double2;
+};
+template <typename R>
+BHA_HD typename Vec2T<R>::type make_v2(double x, double w) {
+  return typename Vec2T<R>::type{R(x), R(w)};
+}
+
+// forward pass: colour, class and (want_grad) the checkpoints. With kStore
+// every state is also kept, rounded to float, in traj[k * stride] and the
+// transmittance before crossing m in cross_t[m * stride] (the FP64 band pass,
+// whose reverse pass runs in FP32 over the stored states).
+template <typename R, typename P, bool kComp, bool kStore = false, typename TS = float>
 BHA_HD void forward(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc, Ckpt<R, kComp>* ck,
-                    int64_t ck_stride, Fwd<R>& f) {
+                    int64_t ck_stride, Fwd<R>& f, typename Vec2T<TS>::type* traj = nullptr, float* cross_t = nullptr,
+                    int64_t store_stride = 0, int max_cross = 0, double2* cross_xw = nullptr) {
   const Rk4Consts<R>& c = consts<R>(p);
   Traj<R> st{rc.x0, rc.w0, kComp ? rc.x0lo : R(0), kComp ? rc.w0lo : R(0)};
   R trans = R(1);
@@ -630,7 +709,12 @@ BHA_HD void forward(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc,
   f.cls = BH_CLASS_MAXSTEPS;
   for (; k < p.kmax; ++k) {
     if (ck && (k & (kSeg - 1)) == 0) ck[(k / kSeg) * ck_stride] = Ckpt<R, kComp>::make(st, trans, m);
+    if (kStore && traj) traj[(int64_t)k * store_stride] = make_v2<TS>(double(st.x), double(st.w));
     if (k == kc) {
+      if (kStore && traj && m < max_cross) {
+        cross_t[(int64_t)m * store_stride] = float(trans);
+        if (cross_xw) cross_xw[(int64_t)m * store_stride] = make_double2(double(st.x), double(st.w));
+      }
       Crossing<R, P> cr;
       if (crossing_eval(s, p, rc, st.x, st.w, dm, kc, cr)) {
         R col[3], dcs[3], dcu[3];
@@ -669,7 +753,9 @@ BHA_HD void forward(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc,
       break;
     }
   }
+  if (kStore && traj) traj[(int64_t)k * store_stride] = make_v2<TS>(double(st.x), double(st.w));
   f.k_end = k;
+  f.m_end = m;
   f.trans = trans;
   for (int i = 0; i < 3; ++i) f.rgb[i] = acc[i];
 }
@@ -830,6 +916,267 @@ BHA_HD void backward(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc
   }
 }
 
+// Backward pass over states stored by forward<..., kStore>, in precision R.
+// p must describe the stored trajectory: for R = float the FP64 step in c32
+// (rounded), inv_h32 and hstep32 (band_view).
+// ---------------------------------------------------------------------------
+// double-float arithmetic (an unevaluated sum hi + lo of two floats, ~48
+// significant bits) by the error-free transformations of Knuth (2Sum) and
+// Dekker (Fast2Sum), with FMA for the exact product error. It runs on the
+// FP32 pipe: on this part an FP64 instruction costs ~80 issue cycles, so a
+// serial FP64 chain is ~5x slower than the same chain in double-float.
+// The error-free transformations need every sum and product rounded on its
+// own: on the device they use the intrinsics the compiler never fuses into an
+// FMA (it would otherwise contract a product into the following sum across
+// inlined calls, and the error terms would be wrong).
+#if defined(__CUDA_ARCH__)
+#define BHA_FADD(a, b) __fadd_rn((a), (b))
+#define BHA_FSUB(a, b) __fsub_rn((a), (b))
+#define BHA_FMUL(a, b) __fmul_rn((a), (b))
+#else
+// host: a rounded store that no compiler fuses
+inline float bha_round(volatile float v) { return v; }
+#define BHA_FADD(a, b) bha_round((a) + (b))
+#define BHA_FSUB(a, b) bha_round((a) - (b))
+#define BHA_FMUL(a, b) bha_round((a) * (b))
+#endif
+struct DF {
+  float hi, lo;
+};
+BHA_HD DF df_fast2sum(float a, float b) {
+  const float s = BHA_FADD(a, b);
+  return DF{s, BHA_FSUB(b, BHA_FSUB(s, a))};
+}
+BHA_HD DF df_add(DF a, DF b) {
+  const float s = BHA_FADD(a.hi, b.hi);
+  const float bb = BHA_FSUB(s, a.hi);
+  const float e = BHA_FADD(BHA_FSUB(a.hi, BHA_FSUB(s, bb)), BHA_FSUB(b.hi, bb));
+  return df_fast2sum(s, BHA_FADD(e, BHA_FADD(a.lo, b.lo)));
+}
+BHA_HD DF df_mul(DF a, DF b) {
+  const float p = BHA_FMUL(a.hi, b.hi);
+  const float e = fmaf(a.hi, b.hi, -p);
+  return df_fast2sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+BHA_HD DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+BHA_HD DF df_mul_f(DF a, float b) {
+  const float p = BHA_FMUL(a.hi, b);
+  const float e = fmaf(a.hi, b, -p);
+  return df_fast2sum(p, fmaf(a.lo, b, e));
+}
+BHA_HD DF df_from(double v) {
+  const float h = float(v);
+  return DF{h, float(v - double(h))};
+}
+BHA_HD double df_to(DF a) { return double(a.hi) + double(a.lo); }
+// a <= b and a < b, exactly
+BHA_HD bool df_le(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+BHA_HD bool df_lt(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+
+// x (3x + 1)
+BHA_HD DF df_fx(DF x) { return df_mul(x, df_add(df_mul_f(x, 3.0f), DF{1.0f, 0.0f})); }
+
+// The RK4 step of step() in double-float.
+BHA_HD void df_step(DF& x, DF& w, const float* k) {
+  const DF h{k[0], k[1]}, hh{k[2], k[3]}, q{k[4], k[5]}, q2{k[6], k[7]}, h26{k[8], k[9]}, h6{k[10], k[11]};
+  const DF k1 = df_fx(x);
+  const DF s1 = df_fma(hh, w, x);
+  const DF k2 = df_fx(s1);
+  const DF s2 = df_fma(q, k1, s1);
+  const DF k3 = df_fx(s2);
+  const DF s3a = df_fma(h, w, x);
+  const DF s3 = df_fma(q2, k2, s3a);
+  const DF k4 = df_fx(s3);
+  const DF A = df_add(k2, k3);
+  const DF S = df_add(A, k1);
+  x = df_fma(h26, S, s3a);
+  w = df_fma(h6, df_add(df_add(S, A), k4), w);
+}
+
+
+inline void set_df_consts(AdjParams* p) {
+  const double v[8] = {p->c64.h, p->c64.hh, p->c64.q, p->c64.q2, p->c64.h26, p->c64.h6, p->c64.x_esc, p->c64.x_hor};
+  for (int i = 0; i < 8; ++i) {
+    const float h = float(v[i]);
+    p->df_c[2 * i] = h;
+    p->df_c[2 * i + 1] = float(v[i] - double(h));
+  }
+}
+
+// forward<double, double, false, true> with the integration in double-float:
+// the same trajectory as the FP64 one to ~1e-14; crossings and the escape
+// are evaluated in FP64 from the converted state.
+BHA_HD void forward_df(const AdjScene& s, const AdjParams& p, const RayC<double, double>& rc, Fwd<double>& f,
+                       float2* traj, float* cross_t, double2* cross_xw, int64_t stride, int max_cross) {
+  DF x = df_from(rc.x0), w = df_from(rc.w0);
+  const DF x_esc{p.df_c[12], p.df_c[13]}, x_hor{p.df_c[14], p.df_c[15]};
+  double trans = 1;
+  double acc[3] = {0, 0, 0};
+  int m = 0;
+  double dm = rc.d0;
+  int kc = s.disc_on ? crossing_step<double, double>(dm, p) : -1;
+  int k = 0;
+  f.cls = BH_CLASS_MAXSTEPS;
+  for (; k < p.kmax; ++k) {
+    if (traj) traj[(int64_t)k * stride] = make_float2(x.hi, w.hi);
+    if (k == kc) {
+      const double xd = df_to(x), wd = df_to(w);
+      if (traj && m < max_cross) {
+        cross_t[(int64_t)m * stride] = float(trans);
+        cross_xw[(int64_t)m * stride] = make_double2(xd, wd);
+      }
+      Crossing<double, double> cr;
+      if (crossing_eval(s, p, rc, xd, wd, dm, kc, cr)) {
+        double col[3], dcs[3], dcu[3];
+        crossing_colour<double, double, PickA<double>>(s, rc, dm, cr, col, dcs, dcu);
+        for (int i = 0; i < 3; ++i) acc[i] = fma(trans * cr.alpha, col[i], acc[i]);
+        trans = trans * (1 - cr.alpha);
+        if (trans < 1e-4) {
+          f.cls = BH_CLASS_DISC;
+          break;
+        }
+      }
+      ++m;
+      dm = rc.d0 + double(m) * kPiD;
+      kc = crossing_step<double, double>(dm, p);
+    }
+    const DF xa = x, wa = w;
+    df_step(x, w, p.df_c);
+    if (!df_lt(x, x_hor)) {  // also NaN
+      f.cls = BH_CLASS_HORIZON;
+      ++k;
+      break;
+    }
+    if (df_le(x, x_esc)) {
+      f.cls = BH_CLASS_MISS;
+      f.xa = df_to(xa);
+      f.wa = df_to(wa);
+      f.xb = df_to(x);
+      f.wb = df_to(w);
+      if (s.has_bg) {
+        Escape<double, double> e;
+        double col[3], dcs[3], dcu[3];
+        escape_eval(s, p, rc, f.xa, f.wa, f.xb, f.wb, k, e, col, dcs, dcu);
+        for (int i = 0; i < 3; ++i) acc[i] = fma(trans, col[i], acc[i]);
+      }
+      ++k;
+      break;
+    }
+  }
+  if (traj) traj[(int64_t)k * stride] = make_float2(x.hi, w.hi);
+  f.k_end = k;
+  f.m_end = m;
+  f.trans = trans;
+  for (int i = 0; i < 3; ++i) f.rgb[i] = acc[i];
+}
+
+// MIXED: whether the ray of pixel (px, py) belongs to the FP64 band,
+// |b/M - 3 sqrt 3| < band. FP64, from b^2 = |F|^2 - (F.e)^2 / |e|^2 (about 20
+// operations); every kernel that needs the decision calls this.
+BHA_HD bool in_band(const AdjScene& s, int px, int py, double band) {
+  const double a = s.half_w - double(px), c = s.half_h - double(py);
+  double e[3], ee = 0, fe = 0, ff = 0;
+  for (int i = 0; i < 3; ++i) {
+    e[i] = fma(s.vz[i], c, fma(s.vy[i], a, s.E0[i]));
+    ee = fma(e[i], e[i], ee);
+    fe = fma(s.F[i], e[i], fe);
+    ff = fma(s.F[i], s.F[i], ff);
+  }
+  const double b2 = fmax(ff - fe * fe / ee, 0.0);
+  return fabs(sqrt(b2) / s.mass - 5.196152422706632) < band;
+}
+
+// Results of an escape adjoint computed elsewhere (in FP64 for the band).
+template <typename R>
+struct EscInit {
+  R Tb, lxa, lwa, lxb, lwb;
+};
+
+// The adjoint of (x0, w0) is returned as lx + clx, lw + clw: for a
+// near-critical ray it is large and nearly orthogonal to the tangents it is
+// contracted with, so its low parts matter. esc (may be null) replaces the
+// escape adjoint (whose contributions to A the caller has added).
+// With x64 (the FP64 ray, parameters, stored crossing states and
+// accumulators) the crossings' adjoints are taken in FP64.
+struct Cross64 {
+  const AdjParams* p;
+  const RayC<double, double>* rc;
+  const double2* xw;
+  const double* ab;
+  Acc<double>* A;
+};
+
+template <typename R, typename P>
+BHA_HD void backward_stored(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc, const Fwd<R>& f,
+                            const R* ab, const typename Vec2T<R>::type* traj, const float* cross_t, int64_t stride,
+                            int max_cross, Acc<R>& A, R& lx, R& lw, R& clx, R& clw, const EscInit<R>* esc = nullptr,
+                            const Cross64* x64 = nullptr) {
+  const Rk4Consts<R>& c = consts<R>(p);
+  const int k_end = f.k_end;
+  R Tb = R(0), lxa = R(0), lwa = R(0);
+  lx = R(0);
+  lw = R(0);
+  if (esc) {
+    Tb = esc->Tb;
+    lxa = esc->lxa;
+    lwa = esc->lwa;
+    lx = esc->lxb;
+    lw = esc->lwb;
+  } else if (f.cls == BH_CLASS_MISS && s.has_bg) {
+    escape_adjoint(s, p, rc, f, ab, Tb, lxa, lwa, lx, lw, A);
+  }
+  // the last crossing taken: index m_end for a disc stop, m_end - 1 otherwise
+  int j = s.disc_on ? (f.cls == BH_CLASS_DISC ? f.m_end : f.m_end - 1) : -1;
+  P dm = rc.d0 + P(j) * P(kPiD);
+  int kc = j >= 0 ? crossing_step<R, P>(dm, p) : -1;
+  clx = R(0);
+  clw = R(0);
+  // the stored states are read 8 at a time ahead of the serial chain
+  constexpr int kAhead = 8;
+  typename Vec2T<R>::type buf[kAhead];
+  for (int k = k_end; k >= 0; --k) {
+    const int slot = (k_end - k) % kAhead;
+    if (slot == 0) {
+#pragma unroll
+      for (int i = 0; i < kAhead; ++i) {
+        const int kk = k - i;
+        if (kk >= 0) buf[i] = traj[(int64_t)kk * stride];
+      }
+    }
+    typename Vec2T<R>::type q = buf[0];
+#pragma unroll
+    for (int i = 1; i < kAhead; ++i)
+      if (slot == i) q = buf[i];
+    if (k < k_end) {
+      step_vjp_comp(q.x, q.y, c, lx, lw, clx, clw);
+      if (k == k_end - 1) {
+        two_sum_acc(lx, lxa, clx);
+        two_sum_acc(lw, lwa, clw);
+      }
+    }
+    while (j >= 0 && kc == k) {
+      const R T = j < max_cross ? R(cross_t[(int64_t)j * stride]) : R(0);
+      R gx = R(0), gw = R(0);
+      if (x64 && j < max_cross) {
+        const double2 xw = x64->xw[(int64_t)j * stride];
+        double Tb64 = double(Tb), gx64 = 0, gw64 = 0;
+        crossing_adjoint(s, *x64->p, *x64->rc, xw.x, xw.y, double(dm), kc, double(T), x64->ab, Tb64, gx64, gw64,
+                         *x64->A);
+        Tb = R(Tb64);
+        gx = R(gx64);
+        gw = R(gw64);
+      } else {
+        crossing_adjoint(s, p, rc, q.x, q.y, dm, kc, T, ab, Tb, gx, gw, A);
+      }
+      two_sum_acc(lx, gx, clx);
+      two_sum_acc(lw, gw, clw);
+      --j;
+      dm = rc.d0 + P(j) * P(kPiD);
+      kc = j >= 0 ? crossing_step<R, P>(dm, p) : -1;
+    }
+  }
+}
+
 // Gradient of the pixel's loss: sum over the ray constants K of dL/dK dK/dtheta_i,
 // dK/dtheta_i by forward-mode tangents of the ray setup.
 template <typename R, typename P>
@@ -922,6 +1269,109 @@ BHA_HD void trace_adjoint(const AdjScene& s, const AdjParams& p, const RayC<R, P
   R lx0, lw0;
   backward<R, P, kComp>(s, p, rc, f, ab, ck, ck_stride, sub, sub_stride, A, lx0, lw0);
   assemble<R, P>(s, R(s.half_w) - R(px), R(s.half_h) - R(py), A, lx0, lw0, out.grad);
+}
+
+// One ray of the FP64 band: forward in FP64 (double-float integration with
+// FP64 events for RR = float) storing every state (in RR), the transmittance
+// and the FP64 state at each crossing; reverse pass in RR over the stored
+// states (pb: the RR view of the FP64 trajectory, see backward_stored) with
+// the escape and crossing adjoints in FP64; tangents of the ray setup in FP64.
+template <typename RR>
+BHA_HD void trace_adjoint_band(const AdjScene& s, const AdjParams& p, const AdjParams& pb, int px, int py,
+                               typename Vec2T<RR>::type* traj, float* cross_t, double2* cross_xw, int64_t stride,
+                               int max_cross, RayOut& out) {
+  const RayC<double, double> rd = ray_constants<double, double>(s, px, py, nullptr);
+  const size_t pix = (size_t)py * s.width + px;
+  const bool grad = p.want_grad && s.target;
+  Fwd<double> f;
+  if constexpr (sizeof(RR) == sizeof(float))
+    forward_df(s, p, rd, f, grad ? traj : nullptr, cross_t, cross_xw, stride, max_cross);
+  else
+    forward<double, double, false, true, RR>(s, p, rd, nullptr, 0, f, grad ? traj : nullptr, cross_t, stride,
+                                             max_cross, cross_xw);
+  out.cls = f.cls;
+  out.steps = f.k_end;
+  for (int i = 0; i < 3; ++i) out.rgb[i] = float(f.rgb[i]);
+  out.loss = 0.f;
+  for (int i = 0; i < kParams; ++i) out.grad[i] = 0.f;
+  if (!s.target) return;
+  RR ab[3];
+  double loss = 0;
+  for (int i = 0; i < 3; ++i) {
+    const double dlt = f.rgb[i] - double(s.target[pix * 3 + i]);
+    loss += dlt * dlt;
+    ab[i] = RR(2 * dlt);
+  }
+  out.loss = float(loss);
+  if (!grad || ((f.cls == BH_CLASS_HORIZON || f.cls == BH_CLASS_MAXSTEPS) && f.trans == 1.0)) return;
+  RayC<RR, double> rf;
+  rf.yv = cast3<RR>(rd.yv);
+  rf.xv = cast3<RR>(rd.xv);
+  rf.x0 = RR(rd.x0);
+  rf.w0 = RR(rd.w0);
+  rf.x0lo = rf.w0lo = RR(0);
+  rf.phi0 = rd.phi0;
+  rf.d0 = rd.d0;
+  rf.M = RR(rd.M);
+  rf.r_in = RR(rd.r_in);
+  rf.r_out = RR(rd.r_out);
+  rf.wsoft = RR(rd.wsoft);
+  Fwd<RR> ff;
+  for (int i = 0; i < 3; ++i) ff.rgb[i] = RR(f.rgb[i]);
+  ff.trans = RR(f.trans);
+  ff.xa = RR(f.xa);
+  ff.wa = RR(f.wa);
+  ff.xb = RR(f.xb);
+  ff.wb = RR(f.wb);
+  ff.cls = f.cls;
+  ff.k_end = f.k_end;
+  ff.m_end = f.m_end;
+  // the escape (the largest adjoint of a near-critical ray) in FP64: its sky
+  // derivative at an FP32 escape direction is off by ~1e-3 there
+  Acc<double> Ae;
+  Ae.yv = Ae.xv = Ae.e2 = V3<double>{0, 0, 0};
+  Ae.phi0 = Ae.d0 = Ae.M = Ae.r_in = Ae.r_out = 0;
+  EscInit<RR> esc{RR(0), RR(0), RR(0), RR(0), RR(0)};
+  const bool escaped = f.cls == BH_CLASS_MISS && s.has_bg;
+  if (escaped) {
+    const double abe[3] = {double(ab[0]), double(ab[1]), double(ab[2])};
+    double Tb, lxa, lwa, lxb, lwb;
+    escape_adjoint(s, p, rd, f, abe, Tb, lxa, lwa, lxb, lwb, Ae);
+    esc = EscInit<RR>{RR(Tb), RR(lxa), RR(lwa), RR(lxb), RR(lwb)};
+  }
+  Acc<RR> A;
+  A.yv = A.xv = A.e2 = V3<RR>{RR(0), RR(0), RR(0)};
+  A.phi0 = A.d0 = A.M = A.r_in = A.r_out = RR(0);
+  // the crossings in FP64 too: from float states their sample point moves by
+  // ~1e-4 texel, which shifts the filtered texture's slope at steep edges
+  const double abd[3] = {double(ab[0]), double(ab[1]), double(ab[2])};
+  Cross64 x64{&p, &rd, cross_xw, abd, &Ae};
+  RR lx0, lw0, clx0, clw0;
+  backward_stored<RR, double>(s, pb, rf, ff, ab, traj, cross_t, stride, max_cross, A, lx0, lw0, clx0, clw0,
+                              escaped ? &esc : nullptr, cross_xw ? &x64 : nullptr);
+  Acc<double> Ad;
+  Ad.yv = cast3<double>(A.yv) + Ae.yv;
+  Ad.xv = cast3<double>(A.xv) + Ae.xv;
+  Ad.e2 = cast3<double>(A.e2) + Ae.e2;
+  Ad.phi0 = A.phi0 + Ae.phi0;
+  Ad.d0 = A.d0 + Ae.d0;
+  Ad.M = A.M + Ae.M;
+  Ad.r_in = A.r_in + Ae.r_in;
+  Ad.r_out = A.r_out + Ae.r_out;
+  assemble<double, double>(s, s.half_w - double(px), s.half_h - double(py), Ad, double(lx0) + double(clx0),
+                           double(lw0) + double(clw0), out.grad);
+}
+
+// Most disc-plane crossings a ray can reach in kmax steps of h.
+inline int max_crossings(int kmax, double h) { return int(kmax * h / kPiD) + 3; }
+
+// The FP32 view of the FP64 trajectory (reverse pass of the band).
+inline AdjParams band_view(const AdjParams& p) {
+  AdjParams b = p;
+  b.c32 = exact_rk4_consts_f32(p.c64.h, p.c64.u_esc, p.kmax);
+  b.inv_h32 = p.inv_h64;
+  b.hstep32 = p.hstep64;
+  return b;
 }
 
 // ---------------------------------------------------------------------------

@@ -71,6 +71,8 @@ struct bh_ctx {
   DevBuf<double> adj_acc;
   PinnedBuf<double> h_adj_acc;
   DevBuf<unsigned long long> adj_counters;
+  cudaStream_t side_stream = nullptr;   // MIXED adjoint: the band pass
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 struct bh_sequence {
@@ -530,6 +532,9 @@ void bh_destroy(bh_ctx* ctx) {
   if (ctx->adj_acc.ptr) cudaFree(ctx->adj_acc.ptr);
   if (ctx->h_adj_acc.ptr) cudaFreeHost(ctx->h_adj_acc.ptr);
   if (ctx->adj_counters.ptr) cudaFree(ctx->adj_counters.ptr);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   if (ctx->ev_staged) cudaEventDestroy(ctx->ev_staged);
@@ -1278,6 +1283,7 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
     }
     a->scene = i;
     a->block_begin = total_blocks;
+    a->ray_begin = total_rays;
     a->target = frames[i].target;
     a->image = frames[i].image;
     a->pixel_grad = frames[i].pixel_grad;
@@ -1301,19 +1307,27 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
   L.p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
   L.p.inv_h32 = 1.0 / double(L.p.c32.h);
   L.p.inv_h64 = 1.0 / o.step;
+  L.p.hstep32 = double(L.p.c32.h);
+  L.p.hstep64 = o.step;
+  set_df_consts(&L.p);
+  L.pband = band_view(L.p);
+  L.max_cross = max_crossings(o.max_steps, o.step);
   L.p.softness = o.softness;
   L.p.band = o.band;
   L.p.kmax = o.max_steps;
   L.p.want_grad = any_target ? 1 : 0;
   L.total_blocks = total_blocks;
+  L.total_rays = total_rays;
   L.ckpt_slots = int64_t(main_grid) * kAdjThreads;
   L.band_slots = int64_t(band_grid) * kAdjThreads;
   const size_t ck_bytes = any_target ? size_t(L.ckpt_slots) * nseg * checkpoint_bytes(o.precision) : 16;
-  const size_t ckb_bytes =
-      any_target && band_grid ? size_t(L.band_slots) * nseg * band_checkpoint_bytes() : 16;
+  const size_t traj_bytes = any_target && band_grid ? size_t(L.band_slots) * (o.max_steps + 1) * sizeof(float2) : 16;
+  const size_t cross_bytes = any_target && band_grid ? size_t(L.band_slots) * L.max_cross * sizeof(float) : 16;
+  const size_t xw_bytes = any_target && band_grid ? size_t(L.band_slots) * L.max_cross * sizeof(double2) : 16;
+  const size_t xw_off = (traj_bytes + cross_bytes + 15) / 16 * 16;
   if ((rc = ensure_dev(ctx, ctx->d_adj, size_t(n)))) return rc;
   if ((rc = ensure_dev(ctx, ctx->adj_ckpt, ck_bytes))) return rc;
-  if ((rc = ensure_dev(ctx, ctx->adj_ckpt_band, ckb_bytes))) return rc;
+  if ((rc = ensure_dev(ctx, ctx->adj_ckpt_band, xw_off + xw_bytes))) return rc;
   if ((rc = ensure_dev(ctx, ctx->adj_acc, size_t(n) * kAccStride))) return rc;
   if ((rc = ensure_pinned(ctx, ctx->h_adj_acc, size_t(n) * kAccStride))) return rc;
   if ((rc = ensure_dev(ctx, ctx->adj_counters, size_t(kCounters)))) return rc;
@@ -1322,7 +1336,9 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
   if ((rc = ensure_dev(ctx, ctx->adj_band, size_t(band_cap)))) return rc;
   L.scenes = ctx->d_adj.ptr;
   L.ckpt = ctx->adj_ckpt.ptr;
-  L.ckpt_band = ctx->adj_ckpt_band.ptr;
+  L.band_traj = reinterpret_cast<float2*>(ctx->adj_ckpt_band.ptr);
+  L.band_cross = reinterpret_cast<float*>(ctx->adj_ckpt_band.ptr + traj_bytes);
+  L.band_cross_xw = reinterpret_cast<double2*>(ctx->adj_ckpt_band.ptr + xw_off);
   L.band_list = ctx->adj_band.ptr;
   L.band_capacity = band_cap;
   L.counters = ctx->adj_counters.ptr;
@@ -1332,7 +1348,12 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
   BH_CUDA(ctx, cudaMemsetAsync(ctx->adj_acc.ptr, 0, sizeof(double) * n * kAccStride, st));
   BH_CUDA(ctx, cudaMemsetAsync(ctx->adj_counters.ptr, 0, sizeof(unsigned long long) * kCounters, st));
   BH_CUDA(ctx, cudaEventRecord(ctx->ev_start, st));
-  BH_CUDA(ctx, launch_adjoint(L, main_grid, band_grid, st));
+  if (o.precision == BH_PRECISION_MIXED && !ctx->side_stream) {
+    BH_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+    BH_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    BH_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  }
+  BH_CUDA(ctx, launch_adjoint(L, main_grid, band_grid, st, ctx->side_stream, ctx->ev_fork, ctx->ev_join));
   BH_CUDA(ctx, cudaEventRecord(ctx->ev_stop, st));
   BH_CUDA(ctx, cudaMemcpyAsync(ctx->h_adj_acc.ptr, ctx->adj_acc.ptr, sizeof(double) * n * kAccStride,
                                cudaMemcpyDeviceToHost, st));
