@@ -266,11 +266,18 @@ def run_ours(args):
 
     launches = 0
 
-    def time_sequence(opts, kernels_per_step):
+    def time_steps(opts, kernels_per_step, graph):
+        """Times one batched render of the 120 frames per step: a replay of
+        the captured sequence (graph) or one bh_render_device call."""
         nonlocal launches
-        seq = r.sequence(cs, frames, opts)
+        if graph:
+            seq = r.sequence(cs, frames, opts)
+            launch, stats = seq.launch, seq.stats
+        else:
+            seq = None
+            launch, stats = (lambda: r.render_device(cs, frames, opts)), r.stats
         for _ in range(args.warmup):
-            seq.launch()
+            launch()
         stream.synchronize()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]
@@ -281,15 +288,16 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 flush.zero_()
             a.record(stream)
-            seq.launch()
+            launch()
             b.record(stream)
         stream.synchronize()
         torch.cuda.synchronize()
         barrier()
         wall = time.perf_counter() - t0
         ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
-        st = seq.stats()
-        seq.close()
+        st = stats()
+        if seq is not None:
+            seq.close()
         launches += kernels_per_step * args.steps
         return max_over_ranks(ms), st, wall
 
@@ -305,17 +313,22 @@ def run_ours(args):
     variants = {}
     clocks = ClockSampler(local)
     clocks.start()
-    ms_tuned, st_tuned, wall_tuned = time_sequence(tuned, 2)
+    # MIXED launches four kernels per render (band classification, the FP64
+    # band pass, the FP32 pass it launches from the device, the host's
+    # draining FP32 launch), the plain tracer one.
+    ms_tuned, st_tuned, wall_tuned = time_steps(tuned, 4, graph=True)
     eq = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
-    for name, opts, k in [
-        ("mixed_batched_step0.01", eq, 2),
-        ("plain_fp32_grid", capi.default_options(precision=capi.PRECISION_FP32), 1),
+    for name, opts, k, graph in [
+        ("mixed_batched_tuned_direct", tuned, 4, False),
+        ("mixed_batched_step0.01", eq, 4, True),
+        ("plain_fp32_grid", capi.default_options(precision=capi.PRECISION_FP32), 1, True),
         ("plain_fp32_persistent", capi.default_options(precision=capi.PRECISION_FP32,
-                                                       schedule=capi.SCHEDULE_PERSISTENT), 1),
+                                                       schedule=capi.SCHEDULE_PERSISTENT), 1, True),
     ]:
-        ms, st, wall = time_sequence(opts, k)
+        ms, st, wall = time_steps(opts, k, graph)
         fp32_steps = st.steps - st.band_steps
-        variants[name] = {"mrays_per_s": round(rays_step * world / (ms * 1e-3) / 1e6, 3),
+        variants[name] = {"call": "bh_sequence_launch" if graph else "bh_render_device",
+                          "mrays_per_s": round(rays_step * world / (ms * 1e-3) / 1e6, 3),
                           "ms_per_step": round(ms, 3), "step": opts.step, "steps_total": int(st.steps),
                           "band_rays": int(st.band_rays),
                           "fp32_tflops": round(fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms * 1e-3) / 1e12, 3),
@@ -327,7 +340,7 @@ def run_ours(args):
     achieved = fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms_tuned * 1e-3) / 1e12
     issue_frac = fp32_steps * capi.RK4_INSTRUCTIONS_PER_STEP / (ms_tuned * 1e-3) / (fp32_tflops * 1e12 / 2)
     variants["mixed_batched_tuned"] = {
-        "mrays_per_s": round(value, 3), "ms_per_step": round(ms_tuned, 3), "step": tuned.step,
+        "call": "bh_sequence_launch", "mrays_per_s": round(value, 3), "ms_per_step": round(ms_tuned, 3), "step": tuned.step,
         "band": tuned.band, "threads_per_block": tuned.threads_per_block,
         "refill_threshold": tuned.refill_threshold, "slice_steps": tuned.slice_steps,
         "steps_total": int(st_tuned.steps), "band_rays": int(st_tuned.band_rays),
@@ -351,6 +364,7 @@ def run_ours(args):
         for _ in range(args.steps):
             r.render_into(cs, hframes, e2e_opts)
         dt = max_over_ranks((time.perf_counter() - t0) / args.steps)
+        launches += 4 * args.steps
         st_e2e = r.stats()
         e2e = {"value": round(rays_step * world / dt / 1e6, 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),

@@ -45,9 +45,17 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _inputs())
 
 
+# Translation units with device-side kernel launches: extensible whole-program
+# device code (whole-program register allocation; the device runtime calls are
+# resolved at the device link against libcudadevrt).
+EWP_SOURCES = {"bh_kernels.cu"}
+
+
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    if src in EWP_SOURCES:
+        cmd.append("-ewp")
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -66,7 +74,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-rdc=true", "-o", tmp, *objs, "-lcudadevrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -198,6 +198,8 @@ int validate_options(bh_ctx* ctx, const bh_render_options& o) {
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
   if (o.band_lanes < 1 || o.band_lanes > 32)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_lanes must be in [1, 32]");
+  if (o.band_serial != 0 && o.band_serial != 1)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_serial must be 0 or 1");
   if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
   if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
@@ -384,6 +386,7 @@ LaunchParams base_params(const bh_render_options& o) {
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;
   p.band_lanes = o.band_lanes;
+  p.band_serial = o.band_serial;
   return p;
 }
 

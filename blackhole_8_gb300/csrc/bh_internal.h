@@ -68,11 +68,13 @@ struct DevCounters {
   unsigned long long band_overflow;
   unsigned long long rays;
   unsigned long long flags;
-  unsigned long long pad[7];
+  unsigned long long blocks_started;  // MIXED FP64 pass: blocks that have begun
+  unsigned long long pad[6];
 };
 
 enum : unsigned long long {
   kFlagBandQueueFull = 1ull << 0,
+  kFlagBandLaunchFailed = 1ull << 1,  // device-side launch of the FP32 pass failed
 };
 
 // Constants of the RK4 integration in one precision, on x = u - 1/3.
@@ -121,11 +123,17 @@ struct LaunchParams {
   int32_t refill_threshold;
   int32_t slice_steps;
   int32_t band_lanes;
+  int32_t band_serial;        // persistent MIXED: 1 = FP32 pass, then FP64 pass, from the host
+  int32_t mixed_blocks;       // persistent MIXED: grid of the FP32 pass the FP64 pass launches (0: none)
 };
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
                         int block_x, int block_y, cudaStream_t stream);
+// MIXED: classifies the FP64-band rays, runs the FP64 pass, which launches
+// the FP32 pass from the device once all its blocks are resident, then a
+// host-launched FP32 pass that drains what is left of the ray queue
+// (band_serial: the FP32 pass, then the FP64 pass, both from the host).
 cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream);
 cudaError_t persistent_occupancy(const LaunchParams& p, int threads, int* blocks_per_sm);
 cudaError_t launch_fp32_probe(float* sink, int blocks, int threads, int iters, cudaStream_t stream);

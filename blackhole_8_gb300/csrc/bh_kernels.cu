@@ -34,6 +34,7 @@
 #include <math_constants.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "bh_internal.h"
@@ -658,6 +659,16 @@ __device__ __noinline__ double eps_fp64(const DevScene& s, int x, int y) {
   return dot(e, e) * (s.mass * s.mass) / dot(fe, fe) - 1.0 / 27.0;
 }
 
+// The FP64 band test of the mixed tracer: an FP32 prefilter on b, then the
+// FP64 first integral of the candidates. setup_mixed and the classification
+// pass make the same decision (same code, same ray).
+__device__ __forceinline__ bool band_candidate(const DevScene& s, const PlaneRay<float>& r, const LaunchParams& p) {
+  return fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band;
+}
+__device__ __forceinline__ bool in_band_eps(double eps, const LaunchParams& p) {
+  return eps > p.eps_band_lo && eps < p.eps_band_hi;
+}
+
 // Sets up one ray of the mixed tracer. Returns false when the ray belongs to
 // the FP64 band (nothing is traced then). Rays within setup_band of b_c take
 // their first integral from FP64; everything else of the setup is FP32.
@@ -665,9 +676,9 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
                                             RayState<float>& st) {
   const PlaneRay<float> r = make_ray<float>(s, x, y);
   init_rk4<float>(s, r, p.c32.h, st);
-  if (fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band) {
+  if (band_candidate(s, r, p)) {
     const double eps = eps_fp64(s, x, y);
-    if (eps > p.eps_band_lo && eps < p.eps_band_hi) return false;
+    if (in_band_eps(eps, p)) return false;
     if (st.status == kRunning) {
       st.eps = float(eps);
       st.w = copysignf(sqrtf(fmaxf(st.eps + st.x * st.x * fmaf(2.f, st.x, 1.f), 0.f)), st.w);
@@ -768,17 +779,40 @@ __device__ __forceinline__ bool take_fp32_ray(const LaunchParams& p, int scene, 
     init_rk4<float>(s, make_ray<float>(s, *px, *py), p.c32.h, st);
     return true;
   }
-  if (setup_mixed(s, *px, *py, p, st)) return true;
-  // deferred to the FP64 pass; the list has one slot per ray of the call
-  const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
-  if (slot < p.band_capacity) p.band_list[slot] = (uint32_t)item;
-  else atomicOr(&p.counters->flags, kFlagBandQueueFull);
-  return false;
+  // a band ray is traced by the FP64 pass (listed by classify_band_kernel)
+  return setup_mixed(s, *px, *py, p, st);
+}
+
+// MIXED: lists the FP64-band rays (global ray indices) before the two passes,
+// with warp-aggregated appends. The list has one slot per ray of the call.
+__global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
+  for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < p.total_rays;
+       item += (long long)gridDim.x * blockDim.x) {
+    const int scene = find_scene(p, item);
+    const DevScene& s = p.scenes[scene];
+    int x, y;
+    bool band = false;
+    if (ray_pixel(s, item - s.ray_begin, &x, &y)) {
+      const PlaneRay<float> r = make_ray<float>(s, x, y);
+      band = band_candidate(s, r, p) && in_band_eps(eps_fp64(s, x, y), p);
+    }
+    const unsigned m = __ballot_sync(__activemask(), band);
+    if (band) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&p.counters->band_count, (unsigned long long)__popc(m));
+      base = __shfl_sync(m, base, leader);
+      const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+      if (slot < p.band_capacity) p.band_list[slot] = (uint32_t)item;
+      else atomicOr(&p.counters->flags, kFlagBandQueueFull);
+    }
+  }
 }
 
 // kPass: 0 = FP32 plain, 1 = FP32 mixed (band rays deferred), 2 = FP64 band.
 template <int kPass>
-__global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
+__device__ __forceinline__ void persistent_body(const LaunchParams& p) {
   using R = typename std::conditional<kPass == 2, double, float>::type;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1;
@@ -875,6 +909,28 @@ __global__ void __launch_bounds__(256) persistent_kernel(LaunchParams p) {
   }
 }
 
+__global__ void __launch_bounds__(256) persistent_plain_kernel(LaunchParams p) { persistent_body<0>(p); }
+
+__global__ void __launch_bounds__(256, 4) persistent_mixed_kernel(LaunchParams p) { persistent_body<1>(p); }
+
+// The FP64 band pass of the mixed tracer, on one block per SM. It is
+// latency-bound: a few long near-critical rays set its length, which is about
+// a third of the tracer's time when it runs after the FP32 pass. Run beside
+// the FP32 pass from its start, the chains hide under the FP32 throughput
+// work, at the cost of the issue slots its FP64 warps take. The block that
+// begins last launches the FP32 pass: every band block is then resident, so
+// the FP32 blocks fill the rest of each SM (and the ones that do not fit
+// start as band blocks exit). The parent completes after its child, so
+// stream order holds.
+__global__ void __launch_bounds__(256) persistent_band_kernel(LaunchParams p) {
+  if (p.mixed_blocks > 0 && threadIdx.x == 0 &&
+      atomicAdd(&p.counters->blocks_started, 1ull) == (unsigned long long)gridDim.x - 1ull) {
+    persistent_mixed_kernel<<<p.mixed_blocks, blockDim.x, 0, cudaStreamFireAndForget>>>(p);
+    if (cudaGetLastError() != cudaSuccess) atomicOr(&p.counters->flags, kFlagBandLaunchFailed);
+  }
+  persistent_body<2>(p);
+}
+
 // ---------------------------------------------------------------------------
 // throughput probes (roofline denominators)
 __global__ void fp32_probe_kernel(float* sink, int iters) {
@@ -924,20 +980,39 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
 
 cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream) {
   if (p.precision == BH_PRECISION_MIXED) {
-    persistent_kernel<1><<<blocks, threads, 0, stream>>>(p);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    persistent_kernel<2><<<blocks, threads, 0, stream>>>(p);
+    // Classification, the FP64 band pass (which launches the FP32 pass
+    // itself, see persistent_band_kernel), then the FP32 pass once more from
+    // the host: it finds the ray queue drained unless the device-side launch
+    // failed.
+    cudaError_t e;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    LaunchParams q = p;
+    q.mixed_blocks = p.band_serial ? 0 : blocks;
+    const int band_blocks = std::max(1, std::min(blocks, sms));
+    const int cg = int(std::min<long long>((q.total_rays + 255) / 256, 8192));
+    classify_band_kernel<<<cg, 256, 0, stream>>>(q);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (p.band_serial) {
+      persistent_mixed_kernel<<<blocks, threads, 0, stream>>>(q);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      persistent_band_kernel<<<band_blocks, threads, 0, stream>>>(q);
+      return cudaGetLastError();
+    }
+    persistent_band_kernel<<<band_blocks, threads, 0, stream>>>(q);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    persistent_mixed_kernel<<<blocks, threads, 0, stream>>>(q);
     return cudaGetLastError();
   }
-  persistent_kernel<0><<<blocks, threads, 0, stream>>>(p);
+  persistent_plain_kernel<<<blocks, threads, 0, stream>>>(p);
   return cudaGetLastError();
 }
 
 cudaError_t persistent_occupancy(const LaunchParams& p, int threads, int* blocks_per_sm) {
   if (p.precision == BH_PRECISION_MIXED)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_kernel<1>, threads, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_kernel<0>, threads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_mixed_kernel, threads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_plain_kernel, threads, 0);
 }
 
 cudaError_t launch_fp32_probe(float* sink, int blocks, int threads, int iters, cudaStream_t stream) {

@@ -162,7 +162,7 @@ int check(const bh_scene* scenes, int32_t n, const bh_device_texture* tex, int32
   if (!(o.step > 0 && o.step <= 1.0) || !(o.band_step > 0 && o.band_step <= 1.0) || o.max_steps < 1 ||
       o.max_steps > 100000000 || !(o.r_escape > 2.0) || !std::isfinite(o.r_escape) || !(o.band >= 0) ||
       !(o.setup_band >= 0) || o.slice_steps < 4 || o.slice_steps > 4096 || o.refill_threshold < 1 ||
-      o.refill_threshold > 32 || o.band_lanes < 1 || o.band_lanes > 32 || o.block_x < 1 || o.block_y < 1 ||
+      o.refill_threshold > 32 || o.band_lanes < 1 || o.band_lanes > 32 || (o.band_serial != 0 && o.band_serial != 1) || o.block_x < 1 || o.block_y < 1 ||
       o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0 || o.threads_per_block < 32 ||
       o.threads_per_block > 256 || o.threads_per_block % 32 != 0 || o.blocks_per_sm < 0 || o.blocks_per_sm > 64)
     return fail(err, len, BH_ERR_INVALID_ARGUMENT, "render options out of range");
@@ -275,6 +275,7 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;
   p.band_lanes = o.band_lanes;
+  p.band_serial = o.band_serial;
 
   if (o.schedule == BH_SCHEDULE_GRID) {
     int32_t w[BH_NOALLOC_MAX_SCENES], h[BH_NOALLOC_MAX_SCENES];

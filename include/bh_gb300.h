@@ -164,7 +164,12 @@ typedef struct bh_render_options {
                                 checks (default 256) */
   int32_t band_lanes;        /* MIXED + PERSISTENT: lanes per warp that trace
                                 FP64 band rays (1..32, default 32) */
-  int32_t reserved[4];
+  int32_t band_serial;       /* MIXED + PERSISTENT: 0 (default) = the FP64 band
+                                pass runs beside the FP32 pass from its start
+                                and launches it from the device; 1 = the FP32
+                                pass, then the FP64 pass, both launched by the
+                                host (each pass on its own, e.g. to profile) */
+  int32_t reserved[3];
 } bh_render_options;
 
 /* Counters of the most recent render on a context. */
@@ -175,7 +180,10 @@ typedef struct bh_render_stats {
   uint64_t band_steps;    /* steps of those rays */
   uint64_t band_overflow; /* band rays that found no slot in the band list
                              (0: the list holds one slot per ray) */
-  uint64_t flags;         /* device error bits (0 = none) */
+  uint64_t flags;         /* device bits (0 = none): 1 = band list full,
+                             2 = MIXED + PERSISTENT: the device-side launch
+                             of the FP32 pass failed and the host's launch
+                             after it traced the bulk (image still complete) */
   double kernel_ms;       /* device time of the launches, CUDA events */
   uint64_t h2d_bytes;     /* bytes copied host -> device by the call */
   uint64_t d2h_bytes;     /* bytes copied device -> host by the call

@@ -51,8 +51,9 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(bh_camera), sizeof(bh_hole), sizeof(bh_disc),
          sizeof(bh_scene), sizeof(bh_frame), sizeof(bh_render_options), sizeof(bh_render_stats),
          offsetof(bh_scene, background));
-  printf("%zu %zu %zu\n", offsetof(bh_render_options, step), offsetof(bh_render_options, band),
-         offsetof(bh_render_options, refill_threshold));
+  printf("%zu %zu %zu %zu %zu\n", offsetof(bh_render_options, step), offsetof(bh_render_options, band),
+         offsetof(bh_render_options, refill_threshold), offsetof(bh_render_options, band_lanes),
+         offsetof(bh_render_options, band_serial));
   return 0;
 }
 ''')
@@ -65,7 +66,8 @@ int main(void) {
                      capi.Scene.background.offset]
     offs = list(map(int, out[1].split()))
     assert offs == [capi.RenderOptions.step.offset, capi.RenderOptions.band.offset,
-                    capi.RenderOptions.refill_threshold.offset]
+                    capi.RenderOptions.refill_threshold.offset, capi.RenderOptions.band_lanes.offset,
+                    capi.RenderOptions.band_serial.offset]
 
 
 def test_create_without_device_reports_no_device(lib):
