@@ -326,6 +326,7 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->half_w_f = float(d->half_w);
   d->half_h_f = float(d->half_h);
   d->inv_mass_f = float(1.0 / d->mass);
+  d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
@@ -375,13 +376,15 @@ LaunchParams base_params(const bh_render_options& o) {
   p.c32 = bhgb::make_rk4_consts<float>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.cband = bhgb::make_rk4_consts<double>(o.band_step, 1.0 / o.r_escape, o.max_steps);
-  p.setup_band = float(o.setup_band);
+  p.setup_band = bhgb::setup_band_for(o.band, o.setup_band);
+  p.class_band = bhgb::class_band_for(o.band);
   {
     const double bc = 3.0 * std::sqrt(3.0);
     const double lo = bc + o.band, hi = bc - o.band;
     p.eps_band_lo = 1.0 / (lo * lo) - 1.0 / 27.0;
     p.eps_band_hi = hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300;
     if (o.band == 0) p.eps_band_lo = p.eps_band_hi = 0.0;  // empty band
+    p.band_key_scale = bhgb::band_key_scale_for(p.eps_band_lo, p.eps_band_hi);
   }
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;
@@ -442,8 +445,8 @@ int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
   p.counters = ctx->d_counters;
   if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
     const uint32_t cap = band_capacity_for(total);
-    if ((rc = ensure_dev(ctx, ctx->band_list, cap))) return rc;
-    p.band_list = ctx->band_list.ptr;
+    if ((rc = ensure_dev(ctx, ctx->band_list, bhgb::band_words(cap)))) return rc;
+    bhgb::carve_band(ctx->band_list.ptr, cap, &p.band_list, &p.band_tmp, &p.band_key);
     p.band_capacity = cap;
   }
   BH_CUDA(ctx, cudaMemcpyAsync(ctx->d_scenes.ptr, ctx->h_scenes.ptr, sizeof(DevScene) * n,
@@ -727,9 +730,9 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
   p.counters = q->d_counters;
   if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
     q->band_capacity = band_capacity_for(total);
-    e = cudaMalloc(&q->band_list, sizeof(uint32_t) * q->band_capacity);
+    e = cudaMalloc(&q->band_list, sizeof(uint32_t) * bhgb::band_words(q->band_capacity));
     if (e != cudaSuccess) return fail(cuda_err(ctx, e, "band list"));
-    p.band_list = q->band_list;
+    bhgb::carve_band(q->band_list, q->band_capacity, &p.band_list, &p.band_tmp, &p.band_key);
     p.band_capacity = q->band_capacity;
   }
   int blocks = 0;

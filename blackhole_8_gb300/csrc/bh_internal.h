@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "bh_gb300.h"
 
 namespace bhgb {
@@ -45,6 +47,7 @@ struct DevScene {
   float dc_f[3], dn_f[3], dv1_f[3], ds1_f[3], ds2_f[3], de1_f[3], de2_f[3];
   float mass_f, b_c_f, r_h_f, r_in_f, r_out_f, s1_len_f, s2_len_f, half_w_f, half_h_f;
   float inv_mass_f;
+  float b_lip;                // bound on |b(x+1) - b(x)| / M along an image row (row_b_lipschitz)
 
   DevTexture disc_tex;
   DevTexture bg_tex;
@@ -70,7 +73,11 @@ struct DevCounters {
   unsigned long long flags;
   unsigned long long blocks_started;  // MIXED FP64 pass: blocks that have begun
   unsigned long long pad[6];
+  // persistent MIXED: the band list's counting sort (kBandKeys buckets of log2 |eps|)
+  unsigned int band_hist[64];
+  unsigned int band_cursor[64];
 };
+constexpr int kBandKeys = 64;
 
 enum : unsigned long long {
   kFlagBandQueueFull = 1ull << 0,
@@ -114,18 +121,66 @@ struct LaunchParams {
   Rk4Consts<double> c64;      // bulk step, FP64
   Rk4Consts<double> cband;    // band step, FP64 (MIXED)
   float setup_band;           // |b - b_c| / M below which MIXED takes eps from FP64
+  float class_band;           // persistent MIXED: |b - b_c| / M (FP32 b) below which the
+                              //   classification takes the FP64 band test (class_band_for)
   double eps_band_lo;         // the FP64 band in terms of eps = 1/(b/M)^2 - 1/27:
   double eps_band_hi;         //   eps(b_c + band) < eps < eps(b_c - band)
   int64_t total_rays;         // persistent: sum of padded scene ray counts
   DevCounters* counters;
-  uint32_t* band_list;        // persistent MIXED: deferred band rays
+  uint32_t* band_list;        // persistent MIXED: band rays, longest first (sorted by |eps|)
+  uint32_t* band_tmp;         //   the classification's unsorted list
+  uint8_t* band_key;          //   and its sort keys
   uint32_t band_capacity;
+  float band_key_scale;       //   1 / |eps| at the band's edge
   int32_t refill_threshold;
   int32_t slice_steps;
   int32_t band_lanes;
   int32_t band_serial;        // persistent MIXED: 1 = FP32 pass, then FP64 pass, from the host
   int32_t mixed_blocks;       // persistent MIXED: grid of the FP32 pass the FP64 pass launches (0: none)
 };
+
+// Bound on how much b / M changes between neighbouring pixels of a row. The
+// ray direction is e = E0 + a vy + c vz (a, c: pixel offsets) and
+// b = |F x e| / |e|, so |db/da| <= |F| |vy| / |e|, and |e| is at least the
+// distance from the origin to the image plane E0 + span(vy, vz). Infinite
+// when that plane passes through the origin (every segment is then tested).
+inline float row_b_lipschitz(const double F[3], const double E0[3], const double vy[3], const double vz[3],
+                             double mass) {
+  const double n[3] = {vy[1] * vz[2] - vy[2] * vz[1], vy[2] * vz[0] - vy[0] * vz[2], vy[0] * vz[1] - vy[1] * vz[0]};
+  const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double dist = nn > 0 ? std::fabs(E0[0] * n[0] + E0[1] * n[1] + E0[2] * n[2]) / nn : 0.0;
+  const double f = std::sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+  const double v = std::sqrt(vy[0] * vy[0] + vy[1] * vy[1] + vy[2] * vy[2]);
+  if (!(dist > 0) || !(mass > 0)) return INFINITY;
+  return float(f * v / (dist * mass));
+}
+
+// The FP32 prefilters on b of the mixed tracer. A band ray has
+// |b - b_c| < band in FP64, and b in FP32 (make_ray) differs from it by
+// ~1e-5 M at most. The classification tests the rays within band + 1e-3 M,
+// the FP32 pass's setup the rays within setup_band, raised to band + 2e-3 M
+// when smaller. Both edges then lie at least 1e-3 M outside the FP64 band, so
+// the two kernels (each with its own compiled make_ray) take the same
+// decision for every ray: only the FP64 band test, the same code in both,
+// decides. The classification then skips the FP64 test for most rays near
+// b_c.
+inline float class_band_for(double band) { return band > 0 ? float(band + 1e-3) : 0.f; }
+inline float setup_band_for(double band, double setup_band) {
+  return float(band > 0 && band + 2e-3 > setup_band ? band + 2e-3 : setup_band);
+}
+
+// The band buffer of the persistent mixed tracer, in 32-bit words: the list,
+// the unsorted list and one key byte per entry, `cap` entries each.
+constexpr size_t band_words(uint32_t cap) { return 2 * size_t(cap) + (size_t(cap) + 3) / 4; }
+inline void carve_band(uint32_t* base, uint32_t cap, uint32_t** list, uint32_t** tmp, uint8_t** key) {
+  *list = base;
+  *tmp = base + cap;
+  *key = reinterpret_cast<uint8_t*>(base + 2 * size_t(cap));
+}
+inline float band_key_scale_for(double eps_lo, double eps_hi) {
+  const double edge = std::fmax(std::fabs(eps_lo), std::fabs(eps_hi));
+  return edge > 0 ? float(1.0 / edge) : 0.f;
+}
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,

@@ -479,12 +479,18 @@ __device__ __forceinline__ bool on_disc(const DevScene& s, RC u) {
 }
 
 // FP64 root refinement of an FP32 crossing whose radius lies within 2e-3 M of
-// a disc edge (out of line).
-__device__ __noinline__ float crossing_u_fp64(const RayState<float>& st, float h, int* hit,
-                                              const DevScene& s) {
-  const double u = crossing_u<double>(st, h);
-  *hit = on_disc<double>(s, u);
-  return float(u);
+// a disc edge (out of line). The state comes by value: a reference would pin
+// the caller's ray state to its stack frame for the whole step loop.
+struct CrossU {
+  float u;
+  int hit;
+};
+__device__ __noinline__ CrossU crossing_u_fp64(float dcr, int kc, float x, float w, float h, const DevScene& s) {
+  const double sc = double(dcr) - double(kc) * double(h);
+  double xd = x, wd = w;
+  rk4_partial<double>(xd, wd, sc);
+  const double u = xd + 1.0 / 3.0;
+  return CrossU{float(u), on_disc<double>(s, u) ? 1 : 0};
 }
 
 // Disc-plane crossing inside step kc. kRefine64: FP32 crossing with FP64
@@ -497,9 +503,9 @@ __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R
     const R rc = BH_S(R, s, mass) / u;
     const R tol = R(2e-3) * BH_S(R, s, mass);
     if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
-      int h64 = 0;
-      u = R(crossing_u_fp64(reinterpret_cast<const RayState<float>&>(st), float(h), &h64, s));
-      hit = h64 != 0;
+      const CrossU r64 = crossing_u_fp64(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
+      u = R(r64.u);
+      hit = r64.hit != 0;
     }
   }
   if (hit) {
@@ -670,15 +676,19 @@ __device__ __forceinline__ bool in_band_eps(double eps, const LaunchParams& p) {
 }
 
 // Sets up one ray of the mixed tracer. Returns false when the ray belongs to
-// the FP64 band (nothing is traced then). Rays within setup_band of b_c take
-// their first integral from FP64; everything else of the setup is FP32.
+// the FP64 band: the lane is left idle (status kDone) and the FP64 pass alone
+// traces and writes the ray. Rays within setup_band of b_c take their first
+// integral from FP64; everything else of the setup is FP32.
 __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, const LaunchParams& p,
                                             RayState<float>& st) {
   const PlaneRay<float> r = make_ray<float>(s, x, y);
   init_rk4<float>(s, r, p.c32.h, st);
   if (band_candidate(s, r, p)) {
     const double eps = eps_fp64(s, x, y);
-    if (in_band_eps(eps, p)) return false;
+    if (in_band_eps(eps, p)) {
+      st.status = kDone;
+      return false;
+    }
     if (st.status == kRunning) {
       st.eps = float(eps);
       st.w = copysignf(sqrtf(fmaxf(st.eps + st.x * st.x * fmaf(2.f, st.x, 1.f), 0.f)), st.w);
@@ -783,30 +793,85 @@ __device__ __forceinline__ bool take_fp32_ray(const LaunchParams& p, int scene, 
   return setup_mixed(s, *px, *py, p, st);
 }
 
-// MIXED: lists the FP64-band rays (global ray indices) before the two passes,
-// with warp-aggregated appends. The list has one slot per ray of the call.
+// Global ray index of pixel (x, y): the inverse of ray_pixel.
+__device__ __forceinline__ long long pixel_ray(const DevScene& s, int x, int y) {
+  const long long tile = (long long)(y >> 2) * s.tiles_x + (x >> 3);
+  return s.ray_begin + tile * 32 + ((y & 3) << 3) + (x & 7);
+}
+
+// Sort key of a band ray: a near-critical ray winds about -ln|eps| / (2 pi)
+// times before it leaves, so its length grows with -log2 |eps|. Four keys per
+// octave of |eps| below the band's edge; the last key takes the rest.
+__device__ __forceinline__ int band_key(double eps, const LaunchParams& p) {
+  const float ae = fmaxf(fabsf(float(eps)) * p.band_key_scale, 1e-30f);
+  return (int)fminf(float(kBandKeys - 1), fmaxf(0.f, -__log2f(ae) * 4.f));
+}
+
+// MIXED: lists the FP64-band rays (global ray indices) before the two passes.
+// One thread per 32-pixel row segment: b / M at the segment's centre (between
+// pixels x0 + 15 and x0 + 16) is within 15.5 b_lip of every pixel's, so only
+// segments whose centre lies within class_band + 15.5 b_lip (+ a rounding
+// margin for the two FP32 evaluations) of b_c / M can hold a band ray. Their
+// pixels take the FP32 pass's own test (make_ray's b, then the FP64 band
+// test), so the listed rays are exactly the ones the FP32 pass leaves out.
+// The band is a ring a few pixels wide; the rest of the frame costs one b per
+// 32 pixels. The list has one slot per ray of the call.
 __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
-  for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < p.total_rays;
-       item += (long long)gridDim.x * blockDim.x) {
-    const int scene = find_scene(p, item);
+  for (int scene = blockIdx.y; scene < p.n_scenes; scene += gridDim.y) {
     const DevScene& s = p.scenes[scene];
-    int x, y;
-    bool band = false;
-    if (ray_pixel(s, item - s.ray_begin, &x, &y)) {
-      const PlaneRay<float> r = make_ray<float>(s, x, y);
-      band = band_candidate(s, r, p) && in_band_eps(eps_fp64(s, x, y), p);
+    const int segs_x = (s.width + 31) >> 5;
+    const long long n_segs = (long long)segs_x * s.height;
+    const V3<float> F = BH_V(float, s, F), E0 = BH_V(float, s, E0);
+    const V3<float> vy = BH_V(float, s, vy), vz = BH_V(float, s, vz);
+    const float Fm = length(F) * s.inv_mass_f;
+    const float reach = p.class_band + 15.5f * s.b_lip + 1e-5f * Fm;
+    for (long long seg = (long long)blockIdx.x * blockDim.x + threadIdx.x; seg < n_segs;
+         seg += (long long)gridDim.x * blockDim.x) {
+      const int y = (int)(seg / segs_x);
+      const int x0 = (int)(seg - (long long)y * segs_x) << 5;
+      const V3<float> e = E0 + vy * (s.half_w_f - (float(x0) + 15.5f)) + vz * (s.half_h_f - float(y));
+      const float bm = length(cross(F, e)) / length(e) * s.inv_mass_f;
+      if (fabsf(bm - float(kBC)) > reach) continue;  // NaN falls through to the test
+      const int x1 = min(x0 + 32, s.width);
+      for (int x = x0; x < x1; ++x) {
+        const PlaneRay<float> r = make_ray<float>(s, x, y);
+        if (!(fabsf(r.b * s.inv_mass_f - float(kBC)) < p.class_band)) continue;
+        const double eps = eps_fp64(s, x, y);
+        if (!in_band_eps(eps, p)) continue;
+        const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
+        if (slot < p.band_capacity) {
+          const int key = band_key(eps, p);
+          p.band_tmp[slot] = (uint32_t)pixel_ray(s, x, y);
+          p.band_key[slot] = (uint8_t)key;
+          atomicAdd(&p.counters->band_hist[key], 1u);
+        } else {
+          atomicOr(&p.counters->flags, kFlagBandQueueFull);
+        }
+      }
     }
-    const unsigned m = __ballot_sync(__activemask(), band);
-    if (band) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(m) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&p.counters->band_count, (unsigned long long)__popc(m));
-      base = __shfl_sync(m, base, leader);
-      const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
-      if (slot < p.band_capacity) p.band_list[slot] = (uint32_t)item;
-      else atomicOr(&p.counters->flags, kFlagBandQueueFull);
+  }
+}
+
+// MIXED: writes the band list in key order, the longest rays (largest keys)
+// first, so that each warp of the FP64 pass takes rays of about the same
+// length (an FP64 warp instruction costs the same with 1 or 32 lanes active)
+// and the longest chains start first. A counting sort: every block scans the
+// histogram, then each entry takes the next slot of its key.
+__global__ void __launch_bounds__(256) sort_band_kernel(LaunchParams p) {
+  __shared__ unsigned base[kBandKeys];
+  if (threadIdx.x == 0) {
+    unsigned run = 0;
+    for (int k = kBandKeys - 1; k >= 0; --k) {
+      base[k] = run;
+      run += p.counters->band_hist[k];
     }
+  }
+  __syncthreads();
+  const unsigned long long n = min(p.counters->band_count, (unsigned long long)p.band_capacity);
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const int k = p.band_key[i];
+    p.band_list[base[k] + atomicAdd(&p.counters->band_cursor[k], 1u)] = p.band_tmp[i];
   }
 }
 
@@ -843,7 +908,13 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
     unsigned idle = __ballot_sync(kFull, st.status == kDone) & usable;
     if (idle == usable && exhausted && pend_mask == 0) break;
     if (__popc(idle) >= thr || idle == usable) {
-      // hand out pending items until every lane is busy or work runs out
+      // Hand out pending items until every lane is busy or work runs out. A
+      // lane takes at most one item per refill: a lane whose item is deferred
+      // (band ray, padding pixel) sits out the round. Handing it the next
+      // item instead would leave the warp holding 31 items of one 8x4 tile
+      // and one of a tile fetched anywhere, and every later refill of the
+      // warp would mix two tiles (+27 % on the FP32 pass at 30 k band rays).
+      unsigned given = 0;
       while (idle) {
         if (pend_mask == 0) {
           if (exhausted) break;
@@ -881,7 +952,8 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
           }
         }
         for (int i = 0; i < n; ++i) pend_mask &= pend_mask - 1u;  // drop the n lowest items
-        idle = __ballot_sync(kFull, st.status == kDone) & usable;
+        given |= __ballot_sync(kFull, ((idle >> lane) & 1u) && rank < n);
+        idle = __ballot_sync(kFull, st.status == kDone) & usable & ~given;
       }
     }
     if (st.status != kDone) {
@@ -991,8 +1063,11 @@ cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cu
     LaunchParams q = p;
     q.mixed_blocks = p.band_serial ? 0 : blocks;
     const int band_blocks = std::max(1, std::min(blocks, sms));
-    const int cg = int(std::min<long long>((q.total_rays + 255) / 256, 8192));
+    // classification: scenes along y, 32-pixel row segments along x
+    const dim3 cg(std::max(1, std::min(sms * 2, 1024)), std::min(q.n_scenes, 65535));
     classify_band_kernel<<<cg, 256, 0, stream>>>(q);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sort_band_kernel<<<sms, 256, 0, stream>>>(q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (p.band_serial) {
       persistent_mixed_kernel<<<blocks, threads, 0, stream>>>(q);

@@ -43,7 +43,7 @@ constexpr size_t round_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign;
 constexpr size_t kCountersOffset = 0;
 constexpr size_t kScenesOffset = round_up(sizeof(DevCounters));
 constexpr size_t kBandOffset = kScenesOffset + round_up(sizeof(DevScene) * BH_NOALLOC_MAX_SCENES);
-constexpr size_t kScratchBytes = kBandOffset + sizeof(uint32_t) * size_t(BH_NOALLOC_MAX_RAYS);
+constexpr size_t kScratchBytes = kBandOffset + sizeof(uint32_t) * bhgb::band_words(BH_NOALLOC_MAX_RAYS);
 
 // The scratch: counters | scene records | band list.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -137,6 +137,7 @@ void resolve(const bh_scene& s, const bh_frame& f, const bh_render_options& o, c
   d->half_w_f = float(d->half_w);
   d->half_h_f = float(d->half_h);
   d->inv_mass_f = float(1.0 / d->mass);
+  d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
@@ -262,15 +263,18 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
   p.c32 = bhgb::make_rk4_consts<float>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.cband = bhgb::make_rk4_consts<double>(o.band_step, 1.0 / o.r_escape, o.max_steps);
-  p.setup_band = float(o.setup_band);
+  p.setup_band = bhgb::setup_band_for(o.band, o.setup_band);
+  p.class_band = bhgb::class_band_for(o.band);
   {
     const double bc = 3.0 * std::sqrt(3.0), lo = bc + o.band, hi = bc - o.band;
     p.eps_band_lo = o.band == 0 ? 0.0 : 1.0 / (lo * lo) - 1.0 / 27.0;
     p.eps_band_hi = o.band == 0 ? 0.0 : (hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300);
+    p.band_key_scale = bhgb::band_key_scale_for(p.eps_band_lo, p.eps_band_hi);
   }
   p.total_rays = total;
   p.counters = reinterpret_cast<DevCounters*>(base + kCountersOffset);
-  p.band_list = reinterpret_cast<uint32_t*>(base + kBandOffset);
+  bhgb::carve_band(reinterpret_cast<uint32_t*>(base + kBandOffset), uint32_t(BH_NOALLOC_MAX_RAYS), &p.band_list,
+                   &p.band_tmp, &p.band_key);
   p.band_capacity = uint32_t(BH_NOALLOC_MAX_RAYS);
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;

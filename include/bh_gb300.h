@@ -159,7 +159,8 @@ typedef struct bh_render_options {
   double band_step;          /* MIXED: RK4 step of the FP64 band (default 0.01) */
   double setup_band;         /* MIXED: rays with |b - 3 sqrt(3) M| < setup_band * M
                                 take their first integral 1/b^2 - 1/27 from FP64
-                                (default 0.1) */
+                                (default 0.1; raised to band + 2e-3 when
+                                smaller) */
   int32_t slice_steps;       /* PERSISTENT: integration steps between refill
                                 checks (default 256) */
   int32_t band_lanes;        /* MIXED + PERSISTENT: lanes per warp that trace
@@ -187,7 +188,7 @@ typedef struct bh_render_stats {
   double kernel_ms;       /* device time of the launches, CUDA events */
   uint64_t h2d_bytes;     /* bytes copied host -> device by the call */
   uint64_t d2h_bytes;     /* bytes copied device -> host by the call
-                             (frames; the 128-byte counters excluded) */
+                             (frames; the counters excluded) */
 } bh_render_stats;
 
 typedef struct bh_ctx bh_ctx;

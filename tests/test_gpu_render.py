@@ -208,25 +208,35 @@ def test_batched_uneven_scenes(renderer):
         assert np.abs(fb.aux[esc] - o["aux"][esc]).max(initial=0) <= 1e-4
 
 
-def test_mixed_band_order_is_bit_exact(renderer):
+@pytest.mark.parametrize("band", [5e-4, 0.05, 0.2])
+def test_mixed_band_order_is_bit_exact(renderer, band):
     """The FP64 band pass beside the FP32 pass (it launches the FP32 pass
     from the device) and the serial order (both passes launched by the host)
     trace every ray with the same code: frames, classes, deflections and
-    counters equal, and no device-side launch failed. The band is widened to
-    0.05 M so that both passes trace rays at this size."""
-    scenes = S.flythrough(4, 160, 90)
+    counters equal, and no device-side launch failed. Every pixel is traced
+    exactly once: the classification (32-pixel row segments, skipped by a
+    bound on b along the row) lists exactly the rays the FP32 pass leaves
+    out, also when the band is wider than setup_band (0.1 M)."""
+    scenes = S.flythrough(4, 160, 90) + S.flythrough(120, 320, 180)[60:64]
+    pixels = sum(s.camera.width() * s.camera.height() for s in scenes)
     res = []
     for serial in (0, 1):
-        o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, band=0.05, band_serial=serial)
+        o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, band=band, band_serial=serial)
         res.append((renderer.render(scenes, o, hit_class=True, aux=True), renderer.stats()))
     (a, sa), (b, sb) = res
     for fa, fb in zip(a, b):
         assert np.array_equal(fa.pixels, fb.pixels)
         assert np.array_equal(fa.hit_class, fb.hit_class)
-        assert np.array_equal(fa.aux, fb.aux)
+        assert np.array_equal(fa.aux.view(np.uint32), fb.aux.view(np.uint32))
     assert (sa.rays, sa.steps, sa.band_rays, sa.band_steps) == (sb.rays, sb.steps, sb.band_rays, sb.band_steps)
-    assert sa.band_rays > 0
+    assert sa.rays == pixels
+    if band >= 0.05:
+        assert sa.band_rays > 0
     assert sa.flags == 0 and sb.flags == 0
+    # the same frames through the grid schedule, which tests the band inline
+    g = renderer.render(scenes, opts(precision=capi.PRECISION_MIXED, band=band), hit_class=True)
+    for fa, fg in zip(a, g):
+        assert (fa.hit_class == fg.hit_class).mean() >= 0.999
 
 
 # ---------------------------------------------------------------------------
