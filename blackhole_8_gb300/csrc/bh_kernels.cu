@@ -808,32 +808,41 @@ __device__ __forceinline__ int band_key(double eps, const LaunchParams& p) {
 }
 
 // MIXED: lists the FP64-band rays (global ray indices) before the two passes.
-// One thread per 32-pixel row segment: b / M at the segment's centre (between
-// pixels x0 + 15 and x0 + 16) is within 15.5 b_lip of every pixel's, so only
-// segments whose centre lies within class_band + 15.5 b_lip (+ a rounding
-// margin for the two FP32 evaluations) of b_c / M can hold a band ray. Their
-// pixels take the FP32 pass's own test (make_ray's b, then the FP64 band
-// test), so the listed rays are exactly the ones the FP32 pass leaves out.
-// The band is a ring a few pixels wide; the rest of the frame costs one b per
-// 32 pixels. The list has one slot per ray of the call.
+// Each lane tests one 32-pixel row segment: b / M at the segment's centre
+// (between pixels x0 + 15 and x0 + 16) is within 15.5 b_lip of every pixel's,
+// so only segments whose centre lies within class_band + 15.5 b_lip (+ a
+// rounding margin for the two FP32 evaluations) of b_c / M can hold a band
+// ray. The warp then takes the pixels of each such segment together, one per
+// lane, with the FP32 pass's own test (make_ray's b, then the FP64 band test),
+// so the listed rays are exactly the ones the FP32 pass leaves out. The band
+// is a ring a few pixels wide: the rest of the frame costs one b per 32
+// pixels. The list has one slot per ray of the call.
 __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (int scene = blockIdx.y; scene < p.n_scenes; scene += gridDim.y) {
     const DevScene& s = p.scenes[scene];
     const int segs_x = (s.width + 31) >> 5;
     const long long n_segs = (long long)segs_x * s.height;
     const V3<float> F = BH_V(float, s, F), E0 = BH_V(float, s, E0);
     const V3<float> vy = BH_V(float, s, vy), vz = BH_V(float, s, vz);
-    const float Fm = length(F) * s.inv_mass_f;
-    const float reach = p.class_band + 15.5f * s.b_lip + 1e-5f * Fm;
-    for (long long seg = (long long)blockIdx.x * blockDim.x + threadIdx.x; seg < n_segs;
-         seg += (long long)gridDim.x * blockDim.x) {
-      const int y = (int)(seg / segs_x);
-      const int x0 = (int)(seg - (long long)y * segs_x) << 5;
-      const V3<float> e = E0 + vy * (s.half_w_f - (float(x0) + 15.5f)) + vz * (s.half_h_f - float(y));
-      const float bm = length(cross(F, e)) / length(e) * s.inv_mass_f;
-      if (fabsf(bm - float(kBC)) > reach) continue;  // NaN falls through to the test
-      const int x1 = min(x0 + 32, s.width);
-      for (int x = x0; x < x1; ++x) {
+    const float reach = p.class_band + 15.5f * s.b_lip + 1e-5f * length(F) * s.inv_mass_f;
+    for (long long base = warp * 32; base < n_segs; base += warps * 32) {
+      const long long seg = base + lane;
+      bool hit = false;
+      if (seg < n_segs) {
+        const int y = (int)(seg / segs_x);
+        const int x0 = (int)(seg - (long long)y * segs_x) << 5;
+        const V3<float> e = E0 + vy * (s.half_w_f - (float(x0) + 15.5f)) + vz * (s.half_h_f - float(y));
+        const float bm = length(cross(F, e)) / length(e) * s.inv_mass_f;
+        hit = !(fabsf(bm - float(kBC)) > reach);  // NaN counts as a hit
+      }
+      for (unsigned hits = __ballot_sync(kFull, hit); hits; hits &= hits - 1u) {
+        const long long hseg = base + (__ffs(hits) - 1);
+        const int y = (int)(hseg / segs_x);
+        const int x = ((int)(hseg - (long long)y * segs_x) << 5) + lane;
+        if (x >= s.width) continue;
         const PlaneRay<float> r = make_ray<float>(s, x, y);
         if (!(fabsf(r.b * s.inv_mass_f - float(kBC)) < p.class_band)) continue;
         const double eps = eps_fp64(s, x, y);
