@@ -63,6 +63,8 @@ def main(argv=None) -> int:
     ap.add_argument("--slice", type=int, default=0)
     ap.add_argument("--refill", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--band-serial", action="store_true",
+                    help="MIXED + persistent: FP32 pass, then FP64 band pass, both host-launched")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ppm", default="")
     args = ap.parse_args(argv)
@@ -80,7 +82,8 @@ def main(argv=None) -> int:
     opts = capi.default_options(integrator=INTEGRATORS[args.integrator], precision=PRECISIONS[args.precision],
                                 schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
                                 band=args.band, setup_band=args.setup_band, slice_steps=args.slice,
-                                refill_threshold=args.refill, threads_per_block=args.threads)
+                                refill_threshold=args.refill, threads_per_block=args.threads,
+                                band_serial=int(args.band_serial))
     with Renderer(0) as r:
         cs = r.c_scenes(scenes)
         import torch

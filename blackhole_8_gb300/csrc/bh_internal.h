@@ -54,6 +54,8 @@ struct DevScene {
   int32_t width, height;
   int32_t disc_on, disc_map, has_bg;
   int32_t tiles_x;            // ceil(W / 8): persistent schedule, 8x4 tiles
+  int32_t tiles_x_shift;      // tile / tiles_x == (tile * tiles_x_magic) >> tiles_x_shift
+  uint64_t tiles_x_magic;     //   for every tile index below 2^31 (DivMagic)
   int64_t ray_begin;          // first ray index of this scene (persistent)
   uint8_t* pixels;
   uint8_t* cls;
@@ -167,6 +169,23 @@ inline float row_b_lipschitz(const double F[3], const double E0[3], const double
 inline float class_band_for(double band) { return band > 0 ? float(band + 1e-3) : 0.f; }
 inline float setup_band_for(double band, double setup_band) {
   return float(band > 0 && band + 2e-3 > setup_band ? band + 2e-3 : setup_band);
+}
+
+// Exact division of 31-bit indices by a fixed divisor d >= 1 with a multiply
+// and a shift (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", 1994): with l = ceil(log2 d), s = 31 + l and
+// m = floor(2^s / d) + 1, floor(n m / 2^s) = floor(n / d) for 0 <= n < 2^31;
+// m < 2^33, so n m fits 64 bits. Frames are at most 32768 x 32768, i.e.
+// below 2^25 tiles.
+struct DivMagic {
+  uint64_t m;
+  int32_t s;
+};
+inline DivMagic div_magic(uint32_t d) {
+  int l = 0;
+  while ((uint64_t(1) << l) < d) ++l;
+  const int s = 31 + l;
+  return {(uint64_t(1) << s) / d + 1, s};
 }
 
 // The band buffer of the persistent mixed tracer, in 32-bit words: the list,

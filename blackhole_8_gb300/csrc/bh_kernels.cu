@@ -767,12 +767,13 @@ __device__ __forceinline__ int find_scene(const LaunchParams& p, long long ray) 
   return lo;
 }
 
-// Pixel of ray `local` (index within its scene).
+// Pixel of ray `local` (index within its scene). The tile index stays below
+// 2^25, so the division by tiles_x is a multiply and a shift (DivMagic).
 __device__ __forceinline__ bool ray_pixel(const DevScene& s, long long local, int* x, int* y) {
-  const long long tile = local >> 5;
+  const unsigned tile = (unsigned)(local >> 5);
   const int l = (int)(local & 31);
-  const int ty = (int)(tile / s.tiles_x);
-  const int tx = (int)(tile - (long long)ty * s.tiles_x);
+  const int ty = (int)(((unsigned long long)tile * s.tiles_x_magic) >> s.tiles_x_shift);
+  const int tx = (int)tile - ty * s.tiles_x;
   *x = tx * 8 + (l & 7);
   *y = ty * 4 + (l >> 3);
   return *x < s.width && *y < s.height;

@@ -99,6 +99,11 @@ void resolve(const bh_scene& s, const bh_frame& f, const bh_render_options& o, c
   d->width = c.width;
   d->height = c.height;
   d->tiles_x = (c.width + 7) / 8;
+  {
+    const bhgb::DivMagic dm = bhgb::div_magic(uint32_t(d->tiles_x));
+    d->tiles_x_magic = dm.m;
+    d->tiles_x_shift = dm.s;
+  }
   d->ray_begin = ray_begin;
   d->disc_on = s.disc.enabled ? 1 : 0;
   if (s.disc.enabled) {
