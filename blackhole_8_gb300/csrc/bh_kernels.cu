@@ -407,12 +407,12 @@ struct RayState {
   R x, w;       // current state
   R xa, wa;     // state before the last step (escape refinement)
   R eps;        // first integral w^2 - x^2 - 2x^3 = 1/b^2 - 1/27 (units of M)
-  R phi0;       // initial in-plane angle of the camera
-  R dcr;        // offset of the next disc-plane crossing from phi0
+  R phi0;       // in-plane angle of the camera from the ray direction (aux only)
+  R dcr;        // angle of the next disc-plane crossing from the camera, phi - phi0
   R ev;         // event payload: u at the disc crossing
   int k, kc;    // steps taken, step index holding the next crossing
   int status;
-  V3<R> yv, xv;
+  V3<R> yv, xv;  // in-plane basis rotated to the camera: position = r (cos(phi - phi0) yv + sin(phi - phi0) xv)
 };
 
 // Sets up the RK4 state from a plane ray computed in precision RS.
@@ -427,17 +427,26 @@ __device__ __forceinline__ double inv_mass<double>(const DevScene& s) { return 1
 template <typename R>
 __device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& ray, R h, RayState<R>& st) {
   const R M = BH_S(R, s, mass);
-  st.yv = ray.yv;
-  st.xv = ray.xv;
   st.k = 0;
   st.kc = 0x7fffffff;
   st.dcr = R(0);
   st.ev = R(0);
   const R bm = ray.b * inv_mass<R>(s);
-  const R x0 = M * rnorm(ray.F0 * ray.F0 + ray.F1 * ray.F1 + ray.b * ray.b) - R(1.0 / 3.0);
-  const R phi0 = atan2(ray.b, ray.F1);
+  const R rr = ray.F1 * ray.F1 + ray.b * ray.b;
+  const R x0 = M * rnorm(ray.F0 * ray.F0 + rr) - R(1.0 / 3.0);
+  // The camera sits at angle phi0 = atan2(b, F1) in the (yv, xv) plane. The
+  // basis rotated by phi0 measures every later angle from the camera, so no
+  // arctangent is needed for phi0 itself (only for the aux output).
+  R c0 = R(1), s0 = R(0);
+  if (rr > R(0)) {
+    const R ir = rnorm(rr);
+    c0 = ray.F1 * ir;
+    s0 = ray.b * ir;
+  }
+  st.yv = ray.yv * c0 + ray.xv * s0;
+  st.xv = ray.xv * c0 - ray.yv * s0;
+  st.phi0 = s.aux ? atan2(ray.b, ray.F1) : R(0);
   st.x = x0;
-  st.phi0 = phi0;
   if (!(bm > R(1e-6))) {  // heads into the centre
     st.status = kHorizon;
     st.w = R(0);
@@ -451,9 +460,11 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& r
   st.status = kRunning;
   if (s.disc_on) {
     const V3<R> n = BH_V(R, s, dn);
-    const R A = dot(n, ray.yv), B = dot(n, ray.xv);
+    const R A = dot(n, st.yv), B = dot(n, st.xv);
     if (A * A + B * B > R(1e-24)) {
-      R d = fmod(atan2(B, A) + kPi<R>() * R(0.5) - phi0, kPi<R>());
+      // the line of nodes: crossings at d + j pi, d in (0, pi]
+      R d = atan2(B, A) + kPi<R>() * R(0.5);
+      if (d > kPi<R>()) d -= kPi<R>();
       if (d <= R(0)) d += kPi<R>();
       st.dcr = d;
       st.kc = (int)floor(d / h);
@@ -591,7 +602,7 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
   if (st.status == kMaxSteps) {
     hit.cls = BH_CLASS_MAXSTEPS;
   } else if (st.status == kDisc) {
-    const R phic = st.phi0 + st.dcr;
+    const R phic = st.dcr;
     const R rw = BH_S(R, s, mass) / st.ev;
     R sp, cp;
     sincos(phic, &sp, &cp);
@@ -617,11 +628,11 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
                  (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
     const R we = dp / c.h;
-    const R phie = st.phi0 + (R(st.k - 1) + t) * c.h;
+    const R phie = (R(st.k - 1) + t) * c.h;  // from the camera
     // direction angle psi = phie + atan2(u, -w) (from the radial direction,
     // measured from yv toward xv); its cosine and sine without atan2
     hit.cls = BH_CLASS_MISS;
-    if (s.aux) hit.aux = float(phie + atan2(c.u_esc, -we) - kPi<R>());
+    if (s.aux) hit.aux = float(st.phi0 + phie + atan2(c.u_esc, -we) - kPi<R>());
     if (s.has_bg) {
       R sp, cp;
       sincos(phie, &sp, &cp);
