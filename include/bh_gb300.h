@@ -274,7 +274,7 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
  * Textures (BGRA8, caller-owned device memory, indexed by the scenes'
  * texture ids) and frames are in device memory; scenes are on the host. The
  * library's own scratch (counters, scene records, the FP64 band list) lives
- * in one fixed device array of about 16 MiB that every device loading the
+ * in one fixed device array of about 34 MiB that every device loading the
  * library holds until exit; calls are limited to BH_NOALLOC_MAX_SCENES scenes
  * and BH_NOALLOC_MAX_RAYS rays (scenes padded to 8x4 tiles) and are rejected
  * with BH_ERR_INVALID_ARGUMENT above that. The first call on a device takes
