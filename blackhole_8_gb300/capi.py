@@ -30,6 +30,7 @@ FORMAT_BGRA8, FORMAT_BGR8, FORMAT_RGBA8 = 0, 1, 2
 TEXEL_BGR8, TEXEL_RGB8, TEXEL_BGRA8, TEXEL_RGBA8 = 0, 1, 2, 3
 SCHEDULE_GRID, SCHEDULE_PERSISTENT = 0, 1
 CLASS_MISS, CLASS_HORIZON, CLASS_DISC, CLASS_MAXSTEPS = 0, 1, 2, 3
+RK4_ALGO_FLOPS_PER_STEP = 50  # BH_RK4_ALGO_FLOPS_PER_STEP: the roofline unit
 RK4_FLOPS_PER_STEP = 28
 RK4_INSTRUCTIONS_PER_STEP = 18
 

@@ -377,9 +377,16 @@ int bh_scene_at_theta(const bh_scene* scene, const double* theta, bh_scene* out)
 int bh_probe_fp32_peak(bh_ctx* ctx, double* tflops, int32_t* sm_count);
 int bh_probe_fp64_peak(bh_ctx* ctx, double* tflops);
 
-/* Algorithmic FP32 flops of one RK4 step of the tracer (FMA = 2). */
+/* Algorithmic FP32 flops of one RK4-in-phi step of the orbit u'' = -u + 3Mu^2
+ * (FMA = 2): four evaluations of f = (w, 3Mu^2 - u) at 3 flops, three stage
+ * states at 2 FMA, the final combination (4 FMA for each of u and w), and
+ * about 10 for the phi advance, the node / horizon / escape compares and the
+ * (cos, sin) rotation recurrence of the 3-D position. The roofline unit. */
+#define BH_RK4_ALGO_FLOPS_PER_STEP 50
+/* What this tracer issues per step: the Runge-Kutta-Nystrom form on
+ * x = u - 1/3 (x'' = x + 3x^2) with events tested by step index, 18 FP32
+ * instructions = 28 flops. */
 #define BH_RK4_FLOPS_PER_STEP 28
-/* FP32 instructions of one RK4 step (Runge-Kutta-Nystrom form). */
 #define BH_RK4_INSTRUCTIONS_PER_STEP 18
 
 #ifdef __cplusplus
