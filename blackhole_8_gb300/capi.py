@@ -22,14 +22,17 @@ BH_ERR_TIMEOUT = -7
 BH_ERR_NO_DEVICE = -8
 BH_ERR_DEVICE_FAULT = -9
 
-INTEGRATOR_REF_TRAPEZOID, INTEGRATOR_RK4 = 0, 1
+INTEGRATOR_REF_TRAPEZOID, INTEGRATOR_RK4, INTEGRATOR_FLAT = 0, 1, 2
 PRECISION_FP32, PRECISION_FP64, PRECISION_MIXED = 0, 1, 2
 RAYGEN_REF, RAYGEN_PINHOLE = 0, 1
 DISC_MAP_REF_PLANAR, DISC_MAP_POLAR = 0, 1
 FORMAT_BGRA8, FORMAT_BGR8, FORMAT_RGBA8 = 0, 1, 2
 TEXEL_BGR8, TEXEL_RGB8, TEXEL_BGRA8, TEXEL_RGBA8 = 0, 1, 2, 3
 SCHEDULE_GRID, SCHEDULE_PERSISTENT = 0, 1
-CLASS_MISS, CLASS_HORIZON, CLASS_DISC, CLASS_MAXSTEPS = 0, 1, 2, 3
+CLASS_MISS, CLASS_HORIZON, CLASS_DISC, CLASS_MAXSTEPS, CLASS_OBJECT = 0, 1, 2, 3, 4
+OBJECT_RECTANGLE, OBJECT_TRIANGLE, OBJECT_PLANE = 1, 2, 3
+MAX_OBJECTS = 64
+ABI_VERSION = 2
 RK4_ALGO_FLOPS_PER_STEP = 50  # BH_RK4_ALGO_FLOPS_PER_STEP: the roofline unit
 RK4_FLOPS_PER_STEP = 28
 RK4_INSTRUCTIONS_PER_STEP = 18
@@ -52,9 +55,14 @@ class Disc(C.Structure):
                 ("mapping", C.c_int32), ("enabled", C.c_int32), ("reserved", C.c_int32)]
 
 
+class Object(C.Structure):
+    _fields_ = [("type", C.c_int32), ("texture", C.c_int32), ("v", D3 * 4), ("axis_x", D3), ("axis_y", D3),
+                ("axis_z", D3), ("pattern_size", C.c_double)]
+
+
 class Scene(C.Structure):
     _fields_ = [("camera", Camera), ("hole", Hole), ("disc", Disc), ("background", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("n_objects", C.c_int32), ("objects", C.POINTER(Object))]
 
 
 class Frame(C.Structure):

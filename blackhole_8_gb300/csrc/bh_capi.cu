@@ -20,6 +20,7 @@
 #include "bh_internal.h"
 
 using bhgb::DevCounters;
+using bhgb::DevObject;
 using bhgb::DevScene;
 using bhgb::DevTexture;
 using bhgb::LaunchParams;
@@ -54,6 +55,8 @@ struct bh_ctx {
   std::vector<TexEntry> textures;
   PinnedBuf<DevScene> h_scenes;
   DevBuf<DevScene> d_scenes;
+  PinnedBuf<DevObject> h_objects;
+  DevBuf<DevObject> d_objects;
   DevCounters* d_counters = nullptr;
   DevCounters* h_counters = nullptr;
   DevBuf<uint32_t> band_list;
@@ -83,6 +86,9 @@ struct bh_sequence {
   std::vector<bh_frame> frames;
   DevScene* h_scenes = nullptr;   // pinned, owned
   DevScene* d_scenes = nullptr;   // owned
+  DevObject* h_objects = nullptr; // pinned, owned (n_objects_total of them)
+  DevObject* d_objects = nullptr; // owned
+  int32_t n_objects_total = 0;
   DevCounters* d_counters = nullptr;
   uint32_t* band_list = nullptr;
   uint32_t band_capacity = 0;
@@ -145,6 +151,11 @@ int ensure_pinned(bh_ctx* ctx, PinnedBuf<T>& b, size_t n) {
 
 bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
 double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+void cross3(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
 
 int bytes_per_pixel(int32_t format) { return format == BH_FORMAT_BGR8 ? 3 : 4; }
 
@@ -169,12 +180,15 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
 }
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
-  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4)
+  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4 &&
+      o.integrator != BH_INTEGRATOR_FLAT)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
   if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
-  if (o.integrator == BH_INTEGRATOR_REF_TRAPEZOID && o.precision == BH_PRECISION_MIXED)
+  if (o.integrator != BH_INTEGRATOR_RK4 && o.precision == BH_PRECISION_MIXED)
     return set_err(ctx, BH_ERR_UNSUPPORTED, "MIXED precision applies to the RK4 integrator only");
+  if (o.integrator == BH_INTEGRATOR_FLAT && o.schedule != BH_SCHEDULE_GRID)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "the FLAT integrator runs on the GRID schedule");
   if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown raygen %d", o.raygen);
   if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8)
@@ -215,6 +229,44 @@ int texture_ok(bh_ctx* ctx, int32_t id) {
   return id >= 0 && id < (int32_t)ctx->textures.size() && ctx->textures[id].alive;
 }
 
+int validate_objects(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_options& o) {
+  if (s.n_objects < 0 || s.n_objects > BH_MAX_OBJECTS)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: n_objects must be in [0, %d]", i, BH_MAX_OBJECTS);
+  if (s.n_objects == 0) return BH_OK;
+  if (!s.objects) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: objects is NULL", i);
+  if (o.schedule != BH_SCHEDULE_GRID || o.precision == BH_PRECISION_MIXED)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: objects need the GRID schedule in FP32 or FP64", i);
+  for (int j = 0; j < s.n_objects; ++j) {
+    const bh_object& b = s.objects[j];
+    if (!finite3(b.v[0]) || !finite3(b.v[1]) || !finite3(b.v[2]) || !finite3(b.v[3]) || !finite3(b.axis_x) ||
+        !finite3(b.axis_y) || !finite3(b.axis_z) || !std::isfinite(b.pattern_size))
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d object %d: non-finite value", i, j);
+    if (b.type == BH_OBJECT_RECTANGLE) {
+      if (b.texture != -1 && !texture_ok(ctx, b.texture))
+        return set_err(ctx, BH_ERR_BAD_TEXTURE, "scene %d object %d: texture %d is not valid", i, j, b.texture);
+      double e1[3], e2[3], n[3];
+      for (int k = 0; k < 3; ++k) {
+        e1[k] = b.v[1][k] - b.v[0][k];
+        e2[k] = b.v[3][k] - b.v[0][k];
+      }
+      cross3(e1, e2, n);
+      if (!(dot3(n, n) > 0))
+        return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d object %d: degenerate rectangle", i, j);
+    } else if (b.type == BH_OBJECT_PLANE) {
+      const double* ax[3] = {b.axis_x, b.axis_y, b.axis_z};
+      for (const double* a : ax)
+        if (!(std::fabs(dot3(a, a) - 1.0) < 1e-6))
+          return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d object %d: plane axes must be unit vectors", i, j);
+      // ChessPattern2D divides by (int)(2 * size)
+      if (b.pattern_size != 0 && !(b.pattern_size >= 0.5))
+        return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d object %d: pattern_size must be 0 or >= 0.5", i, j);
+    } else if (b.type != BH_OBJECT_TRIANGLE) {
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d object %d: unknown type %d", i, j, b.type);
+    }
+  }
+  return BH_OK;
+}
+
 int validate_scene(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_options& o) {
   const bh_camera& c = s.camera;
   if (c.width < 1 || c.height < 1 || c.width > 32768 || c.height > 32768)
@@ -226,6 +278,7 @@ int validate_scene(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_option
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: hole mass must be positive and finite", i);
   if (s.background != -1 && !texture_ok(ctx, s.background))
     return set_err(ctx, BH_ERR_BAD_TEXTURE, "scene %d: background texture %d is not valid", i, s.background);
+  if (int rc = validate_objects(ctx, s, i, o)) return rc;
   const double rel[3] = {c.position[0] - s.hole.position[0], c.position[1] - s.hole.position[1],
                          c.position[2] - s.hole.position[2]};
   if (o.integrator == BH_INTEGRATOR_RK4 && std::sqrt(dot3(rel, rel)) >= o.r_escape * s.hole.mass)
@@ -337,6 +390,32 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->aux = f.aux;
 }
 
+int32_t count_objects(const bh_scene* scenes, int32_t n) {
+  int32_t t = 0;
+  for (int i = 0; i < n; ++i) t += scenes[i].n_objects;
+  return t;
+}
+
+// Resolves the objects of all scenes, in table order, into h and points each
+// scene record at its own run of them in d.
+void resolve_objects(bh_ctx* ctx, const bh_scene* scenes, int32_t n, DevObject* h, const DevObject* d,
+                     DevScene* recs) {
+  int32_t at = 0;
+  for (int i = 0; i < n; ++i) {
+    recs[i].objects = scenes[i].n_objects > 0 ? d + at : nullptr;
+    recs[i].n_objects = scenes[i].n_objects;
+    for (int j = 0; j < scenes[i].n_objects; ++j, ++at) {
+      const bh_object& b = scenes[i].objects[j];
+      DevTexture t{nullptr, 0, 0};
+      if (b.type == BH_OBJECT_RECTANGLE && b.texture >= 0) {
+        const TexEntry& e = ctx->textures[b.texture];
+        t = DevTexture{e.texels, e.width, e.height};
+      }
+      bhgb::resolve_object(b, scenes[i].hole.position, t, h + at);
+    }
+  }
+}
+
 int64_t padded_rays(const bh_camera& c) {
   return int64_t((c.width + 7) / 8) * int64_t((c.height + 3) / 4) * 32;
 }
@@ -354,8 +433,8 @@ int check_inputs(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame*
     rc = validate_scene(ctx, scenes[i], i, *o);
     if (rc) return rc;
     if (!frames[i].pixels) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "frame %d has no pixel buffer", i);
-    if (frames[i].aux && o->integrator != BH_INTEGRATOR_RK4)
-      return set_err(ctx, BH_ERR_UNSUPPORTED, "frame %d: aux output needs the RK4 integrator", i);
+    if (frames[i].aux && o->integrator == BH_INTEGRATOR_REF_TRAPEZOID)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "frame %d: aux output needs the RK4 or FLAT integrator", i);
     total += padded_rays(scenes[i].camera);
   }
   if (total >= (int64_t(1) << 32)) return set_err(ctx, BH_ERR_UNSUPPORTED, "too many rays in one call");
@@ -421,7 +500,8 @@ int enqueue_kernels(bh_ctx* ctx, LaunchParams& p, const bh_render_options& o, co
       w[i] = scenes[i].camera.width;
       h[i] = scenes[i].camera.height;
     }
-    BH_CUDA(ctx, bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, st));
+    const bool objects = o.integrator == BH_INTEGRATOR_FLAT || count_objects(scenes, n) > 0;
+    BH_CUDA(ctx, bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, st, objects));
   } else {
     int blocks = 0;
     int rc = persistent_blocks(ctx, p, o, &blocks);
@@ -443,6 +523,12 @@ int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
     resolve_scene(ctx, scenes[i], dframes[i], o, total, ctx->h_scenes.ptr + i);
     total += padded_rays(scenes[i].camera);
   }
+  const int32_t nobj = count_objects(scenes, n);
+  if (nobj > 0) {
+    if ((rc = ensure_pinned(ctx, ctx->h_objects, nobj))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->d_objects, nobj))) return rc;
+    resolve_objects(ctx, scenes, n, ctx->h_objects.ptr, ctx->d_objects.ptr, ctx->h_scenes.ptr);
+  }
   LaunchParams p = base_params(o);
   p.scenes = ctx->d_scenes.ptr;
   p.n_scenes = n;
@@ -454,9 +540,12 @@ int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
     bhgb::carve_band(ctx->band_list.ptr, cap, &p.band_list, &p.band_tmp, &p.band_key);
     p.band_capacity = cap;
   }
+  if (nobj > 0)
+    BH_CUDA(ctx, cudaMemcpyAsync(ctx->d_objects.ptr, ctx->h_objects.ptr, sizeof(DevObject) * nobj,
+                                 cudaMemcpyHostToDevice, st));
   BH_CUDA(ctx, cudaMemcpyAsync(ctx->d_scenes.ptr, ctx->h_scenes.ptr, sizeof(DevScene) * n,
                                cudaMemcpyHostToDevice, st));
-  ctx->h2d_bytes = sizeof(DevScene) * size_t(n);
+  ctx->h2d_bytes = sizeof(DevScene) * size_t(n) + sizeof(DevObject) * size_t(nobj);
   ctx->d2h_bytes = 0;
   BH_CUDA(ctx, cudaEventRecord(ctx->ev_staged, st));
   ctx->staged_pending = true;
@@ -531,6 +620,8 @@ void bh_destroy(bh_ctx* ctx) {
     if (t.texels) cudaFree(t.texels);
   if (ctx->h_scenes.ptr) cudaFreeHost(ctx->h_scenes.ptr);
   if (ctx->d_scenes.ptr) cudaFree(ctx->d_scenes.ptr);
+  if (ctx->h_objects.ptr) cudaFreeHost(ctx->h_objects.ptr);
+  if (ctx->d_objects.ptr) cudaFree(ctx->d_objects.ptr);
   if (ctx->band_list.ptr) cudaFree(ctx->band_list.ptr);
   if (ctx->out_arena.ptr) cudaFree(ctx->out_arena.ptr);
   if (ctx->d_counters) cudaFree(ctx->d_counters);
@@ -722,12 +813,18 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
   if (e == cudaSuccess) e = cudaMalloc(&q->d_scenes, sizeof(DevScene) * n);
   if (e == cudaSuccess) e = cudaMalloc(&q->d_counters, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&q->ev_done, cudaEventDisableTiming);
+  q->n_objects_total = count_objects(scenes, n);
+  if (e == cudaSuccess && q->n_objects_total > 0) {
+    e = cudaMallocHost(&q->h_objects, sizeof(DevObject) * q->n_objects_total);
+    if (e == cudaSuccess) e = cudaMalloc(&q->d_objects, sizeof(DevObject) * q->n_objects_total);
+  }
   if (e != cudaSuccess) return fail(cuda_err(ctx, e, "sequence buffers"));
   int64_t total = 0;
   for (int i = 0; i < n; ++i) {
     resolve_scene(ctx, scenes[i], frames[i], o, total, q->h_scenes + i);
     total += padded_rays(scenes[i].camera);
   }
+  if (q->n_objects_total > 0) resolve_objects(ctx, scenes, n, q->h_objects, q->d_objects, q->h_scenes);
   LaunchParams p = base_params(o);
   p.scenes = q->d_scenes;
   p.n_scenes = n;
@@ -746,6 +843,9 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
   e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(cuda_err(ctx, e, "capture stream"));
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess && q->n_objects_total > 0)
+    e = cudaMemcpyAsync(q->d_objects, q->h_objects, sizeof(DevObject) * q->n_objects_total, cudaMemcpyHostToDevice,
+                        cs);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(q->d_scenes, q->h_scenes, sizeof(DevScene) * n, cudaMemcpyHostToDevice, cs);
   if (e == cudaSuccess) e = cudaMemsetAsync(q->d_counters, 0, sizeof(DevCounters), cs);
@@ -756,7 +856,8 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
         w[i] = scenes[i].camera.width;
         h[i] = scenes[i].camera.height;
       }
-      e = bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, cs);
+      e = bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, cs,
+                            o.integrator == BH_INTEGRATOR_FLAT || q->n_objects_total > 0);
     } else {
       e = bhgb::launch_persistent(p, o.threads_per_block, blocks, cs);
     }
@@ -785,8 +886,9 @@ int bh_sequence_update(bh_sequence* q, const bh_scene* scenes, int32_t n) {
     const bh_scene& b = q->scenes[i];
     if (a.camera.width != b.camera.width || a.camera.height != b.camera.height ||
         a.background != b.background || a.disc.enabled != b.disc.enabled ||
-        (a.disc.enabled && a.disc.texture != b.disc.texture))
-      return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d changes sizes or textures of the sequence", i);
+        (a.disc.enabled && a.disc.texture != b.disc.texture) || a.n_objects != b.n_objects)
+      return set_err(ctx, BH_ERR_INVALID_ARGUMENT,
+                     "scene %d changes sizes, textures or the object count of the sequence", i);
     int rc = validate_scene(ctx, a, i, q->opts);
     if (rc) return rc;
   }
@@ -798,6 +900,7 @@ int bh_sequence_update(bh_sequence* q, const bh_scene* scenes, int32_t n) {
     total += padded_rays(scenes[i].camera);
     q->scenes[i] = scenes[i];
   }
+  if (q->n_objects_total > 0) resolve_objects(ctx, scenes, n, q->h_objects, q->d_objects, q->h_scenes);
   return BH_OK;
 }
 
@@ -839,6 +942,8 @@ void bh_sequence_destroy(bh_sequence* q) {
   if (q->graph) cudaGraphDestroy(q->graph);
   if (q->h_scenes) cudaFreeHost(q->h_scenes);
   if (q->d_scenes) cudaFree(q->d_scenes);
+  if (q->h_objects) cudaFreeHost(q->h_objects);
+  if (q->d_objects) cudaFree(q->d_objects);
   if (q->d_counters) cudaFree(q->d_counters);
   if (q->band_list) cudaFree(q->band_list);
   if (q->ev_done) cudaEventDestroy(q->ev_done);
@@ -1268,6 +1373,8 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
     } else {
       base_theta(scenes[i], th);
     }
+    if (scenes[i].n_objects != 0)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: the differentiable render draws no objects", i);
     bh_scene posed;
     scene_at_theta(scenes[i], th, &posed);
     if ((rc = validate_scene(ctx, posed, i, ro))) return rc;

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <cstring>
 
 #include "bh_gb300.h"
 
@@ -16,6 +17,25 @@ struct DevTexture {
   const uchar4* texels;
   int32_t width;
   int32_t height;
+};
+
+// An ordinary object (bh_object) resolved for the device: positions relative
+// to the hole, in FP64 and rounded once to FP32.
+struct DevObject {
+  double p0[3];   // RECTANGLE, TRIANGLE: vertex()[1]; PLANE: position()
+  double e1[3];   // RECTANGLE: vertex()[2] - vertex()[1]; TRIANGLE: vertex()[2] - vertex()[1]
+  double e2[3];   // RECTANGLE: vertex()[4] - vertex()[1]; TRIANGLE: vertex()[3] - vertex()[1]
+  double n[3];    // RECTANGLE: normalize(e1 x e2); PLANE: vector_z()
+  double ax[3];   // PLANE: vector_x()
+  double ay[3];   // PLANE: vector_y()
+  double hw[3];   // PLANE: the hole's world position (the colour takes world x, y)
+  double e1_len, e2_len;  // RECTANGLE: |e1|, |e2|
+  double pattern;         // PLANE: ChessPattern2D size (<= 0: black)
+  float p0_f[3], e1_f[3], e2_f[3], n_f[3], ax_f[3], ay_f[3], hw_f[3];
+  float e1_len_f, e2_len_f, pattern_f;
+  DevTexture tex;         // RECTANGLE: texels, or null (black)
+  int32_t type;           // BH_OBJECT_*
+  int32_t pad;
 };
 
 // One scene resolved for the device. Positions are relative to the hole.
@@ -57,6 +77,9 @@ struct DevScene {
   int32_t tiles_x_shift;      // tile / tiles_x == (tile * tiles_x_magic) >> tiles_x_shift
   uint64_t tiles_x_magic;     //   for every tile index below 2^31 (DivMagic)
   int64_t ray_begin;          // first ray index of this scene (persistent)
+  const DevObject* objects;   // this scene's objects (n_objects of them)
+  int32_t n_objects;
+  int32_t pad_objects;
   uint8_t* pixels;
   uint8_t* cls;
   float* aux;
@@ -171,6 +194,51 @@ inline float setup_band_for(double band, double setup_band) {
   return float(band > 0 && band + 2e-3 > setup_band ? band + 2e-3 : setup_band);
 }
 
+// Resolves a bh_object for the device, relative to the hole at h (host).
+// Edges are formed in world coordinates as the reference forms them;
+// the rectangle's normal is cv::normalize(e1 x e2) = v * (1 / |v|).
+inline void resolve_object(const bh_object& b, const double h[3], DevTexture tex, DevObject* d) {
+  std::memset(d, 0, sizeof(*d));
+  d->type = b.type;
+  auto put = [](double* dst, float* dstf, const double* v) {
+    for (int k = 0; k < 3; ++k) {
+      dst[k] = v[k];
+      dstf[k] = float(v[k]);
+    }
+  };
+  const double p0[3] = {b.v[0][0] - h[0], b.v[0][1] - h[1], b.v[0][2] - h[2]};
+  put(d->p0, d->p0_f, p0);
+  if (b.type == BH_OBJECT_PLANE) {
+    put(d->n, d->n_f, b.axis_z);
+    put(d->ax, d->ax_f, b.axis_x);
+    put(d->ay, d->ay_f, b.axis_y);
+    put(d->hw, d->hw_f, h);
+    d->pattern = b.pattern_size;
+    d->pattern_f = float(b.pattern_size);
+    return;
+  }
+  const int third = b.type == BH_OBJECT_RECTANGLE ? 3 : 2;
+  double e1[3], e2[3];
+  for (int k = 0; k < 3; ++k) {
+    e1[k] = b.v[1][k] - b.v[0][k];
+    e2[k] = b.v[third][k] - b.v[0][k];
+  }
+  put(d->e1, d->e1_f, e1);
+  put(d->e2, d->e2_f, e2);
+  if (b.type == BH_OBJECT_RECTANGLE) {
+    const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double k = len > 0 ? 1.0 / len : 0.0;
+    const double nn[3] = {n[0] * k, n[1] * k, n[2] * k};
+    put(d->n, d->n_f, nn);
+    d->e1_len = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    d->e2_len = std::sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
+    d->e1_len_f = float(d->e1_len);
+    d->e2_len_f = float(d->e2_len);
+    d->tex = tex;
+  }
+}
+
 // Exact division of 31-bit indices by a fixed divisor d >= 1 with a multiply
 // and a shift (Granlund and Montgomery, "Division by invariant integers
 // using multiplication", 1994): with l = ceil(log2 d), s = 31 + l and
@@ -202,8 +270,9 @@ inline float band_key_scale_for(double eps_lo, double eps_hi) {
 }
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.
+// objects: the FLAT integrator or a scene with objects (grid_objects_kernel).
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
-                        int block_x, int block_y, cudaStream_t stream);
+                        int block_x, int block_y, cudaStream_t stream, bool objects = false);
 // MIXED: classifies the FP64-band rays, runs the FP64 pass, which launches
 // the FP32 pass from the device once all its blocks are resident, then a
 // host-launched FP32 pass that drains what is left of the ray queue

@@ -90,8 +90,8 @@ struct Pick<double> {
   static __device__ __forceinline__ V3<double> v(const double* d, const float*) { return {d[0], d[1], d[2]}; }
   static __device__ __forceinline__ double s(double d, float) { return d; }
 };
-#define BH_V(R, s, name) Pick<R>::v((s).name, (s).name##_f)
-#define BH_S(R, s, name) Pick<R>::s((s).name, (s).name##_f)
+#define BH_V(R, obj, name) Pick<R>::v((obj).name, (obj).name##_f)
+#define BH_S(R, obj, name) Pick<R>::s((obj).name, (obj).name##_f)
 
 template <typename R>
 __device__ __forceinline__ R kPi() { return R(CUDART_PI); }
@@ -115,16 +115,19 @@ __device__ __forceinline__ int trunc_to_int(double v) {
 // truncating casts, linear index px_h * cols + px_w (clamped to the texture
 // where the reference reads out of bounds).
 template <typename R>
-__device__ uchar4 disc_color_planar(const DevScene& s, V3<R> hit) {
-  const V3<R> s1 = BH_V(R, s, ds1);
-  const V3<R> v = hit - BH_V(R, s, dv1);
+__device__ uchar4 quad_texel(const DevTexture& t, V3<R> v1, V3<R> s1, R s1l, R s2l, V3<R> hit) {
+  const V3<R> v = hit - v1;
   const R r = length(v);
-  const R s1l = BH_S(R, s, s1_len);
   R th = acos(dot(s1, v) / (s1l * r));
   th = (th == th) ? th : R(0);
-  const int px_w = trunc_to_int(double(r * cos(th) / s1l) * s.disc_tex.width);
-  const int px_h = trunc_to_int(double(r * sin(th) / BH_S(R, s, s2_len)) * s.disc_tex.height);
-  return texel(s.disc_tex, (long long)px_h * s.disc_tex.width + px_w);
+  const int px_w = trunc_to_int(double(r * cos(th) / s1l) * t.width);
+  const int px_h = trunc_to_int(double(r * sin(th) / s2l) * t.height);
+  return texel(t, (long long)px_h * t.width + px_w);
+}
+
+template <typename R>
+__device__ uchar4 disc_color_planar(const DevScene& s, V3<R> hit) {
+  return quad_texel<R>(s.disc_tex, BH_V(R, s, dv1), BH_V(R, s, ds1), BH_S(R, s, s1_len), BH_S(R, s, s2_len), hit);
 }
 
 // Polar disc mapping: x over [r_in, r_out], y over the azimuth about e1.
@@ -237,13 +240,141 @@ __device__ R solve_g(R b, R M) {
 
 // Nearest collision on the chord p1 -> p2; the hole is tested first (the
 // iteration order of the reference's two-object map), ties keep it.
+// ---------------------------------------------------------------------------
+// ordinary objects (bh_object) on a chord p1 -> p2, in precision R
+
 template <typename R>
+__device__ __forceinline__ V3<R> div3(V3<R> a, R d) { return {a.x / d, a.y / d, a.z / d}; }
+
+// ChessPattern2D<T>{size} (pattern.h:23-46): white or black by the parity of
+// the cells containing (x, y), mirrored across the axes. The (int) casts are
+// pinned for non-finite and huge values.
+template <typename R>
+__device__ uchar4 chess(R size, R x, R y) {
+  const R two = size * R(2);
+  const int m = trunc_to_int(double(two));
+  if (m == 0) return make_uchar4(0, 0, 0, 255);
+  const R bx = fabs(x), by = fabs(y);
+  const R x2 = bx - R(trunc_to_int(double(bx)) / m) * two;
+  const R y2 = by - R(trunc_to_int(double(by)) / m) * two;
+  const bool in = (x2 <= size && y2 <= size) || (size <= x2 && size <= y2);
+  const bool white = (x * y > R(0)) ? in : !in;
+  return white ? make_uchar4(255, 255, 255, 255) : make_uchar4(0, 0, 0, 255);
+}
+
+// Colour of a hit on an object (hit relative to the hole).
+template <typename R>
+__device__ uchar4 object_color(const DevObject& o, V3<R> hit) {
+  if (o.type == BH_OBJECT_RECTANGLE) {
+    if (!o.tex.texels) return make_uchar4(0, 0, 0, 255);
+    // Rectangle::color (vector_object.h:163-180)
+    return quad_texel<R>(o.tex, BH_V(R, o, p0), BH_V(R, o, e1), BH_S(R, o, e1_len), BH_S(R, o, e2_len), hit);
+  }
+  if (o.type == BH_OBJECT_PLANE) {
+    const R size = BH_S(R, o, pattern);
+    if (!(size > R(0))) return make_uchar4(0, 0, 0, 255);
+    // InfinitePlane::color (vector_object.h:227-232): plane coordinates
+    // from the world x and y of the hit
+    const V3<R> w = hit + BH_V(R, o, hw);
+    const V3<R> ax = BH_V(R, o, ax), ay = BH_V(R, o, ay);
+    const R b = (ax.x * w.y - ax.y * w.x) / (ax.x * ay.y - ax.y * ay.x);
+    const R a = (w.x - b * ay.x) / ax.x;
+    return chess<R>(size, a, b);
+  }
+  return make_uchar4(0, 0, 0, 255);  // Triangle: Material::color (material.h:54)
+}
+
+// Object::Collide of each type (points relative to the hole).
+template <typename R>
+__device__ bool object_collide(const DevObject& o, V3<R> a, V3<R> b, V3<R>* hit) {
+  const V3<R> p0 = BH_V(R, o, p0);
+  if (o.type == BH_OBJECT_RECTANGLE) {
+    // Rectangle::Collide (vector_object.h:107-127): the chord crosses the
+    // quad's plane inside the parallelogram on v1, v2 - v1, v4 - v1
+    const V3<R> e1 = BH_V(R, o, e1), e2 = BH_V(R, o, e2), n = BH_V(R, o, n);
+    const V3<R> Q1 = a - p0, Q2 = b - p0;
+    const R q1 = dot(n, Q1), q2 = dot(n, Q2);
+    if (!(q1 * q2 < R(0))) return false;
+    const R a1 = fabs(q1), a2 = fabs(q2);
+    const V3<R> Q = div3(Q1 * a2 + Q2 * a1, a1 + a2);
+    const R d1 = dot(e1, Q), d2 = dot(e2, Q);
+    if (d1 > R(0) && dot(e1, e1) > d1 && d2 > R(0) && dot(e2, e2) > d2) {
+      *hit = Q + p0;
+      return true;
+    }
+    return false;
+  }
+  if (o.type == BH_OBJECT_TRIANGLE) {
+    // Triangle::Collide (vector_object.h:39-71), Moller-Trumbore; as in the
+    // reference, t has no upper bound: a hit may lie past the chord's end
+    const R ep = R(sizeof(R) == 8 ? 2.220446049250313e-15 : 1.1920928955078125e-06);
+    const V3<R> rv = b - a;
+    const V3<R> e1 = BH_V(R, o, e1), e2 = BH_V(R, o, e2);
+    const V3<R> h = cross(rv, e2);
+    const R det = dot(e1, h);
+    if (-ep < det && det < ep) return false;
+    const R f = R(1) / det;
+    const V3<R> sv = a - p0;
+    const R u = f * dot(sv, h);
+    if (u < R(0) || u > R(1)) return false;
+    const V3<R> q = cross(sv, e1);
+    const R v = f * dot(rv, q);
+    if (v < R(0) || u + v > R(1)) return false;
+    const R t = f * dot(e2, q);
+    if (t <= ep) return false;
+    *hit = a + rv * t;
+    return true;
+  }
+  // InfinitePlane::Collide (vector_object.h:210-225)
+  const V3<R> n = BH_V(R, o, n);
+  const R t1 = dot(n, a - p0), t2 = dot(n, b - p0);
+  if (t1 * t2 > R(0)) return false;
+  const R d1 = fabs(t1), d2 = fabs(t2);
+  *hit = div3(a * d2 + b * d1, d1 + d2);
+  return true;
+}
+
+// The object hit nearest a on the chord a -> b, visiting the objects from
+// last to first and keeping the first on ties; -1 when none.
+template <typename R>
+__device__ int nearest_object(const DevScene& s, V3<R> a, V3<R> b, R* dd_out, V3<R>* hit) {
+  int obj = -1;
+  R best = R(0);
+  for (int i = s.n_objects - 1; i >= 0; --i) {
+    V3<R> h;
+    if (object_collide<R>(s.objects[i], a, b, &h)) {
+      const V3<R> d = a - h;
+      const R dd = dot(d, d);
+      if (obj < 0 || dd < best) {
+        best = dd;
+        *hit = h;
+        obj = i;
+      }
+    }
+  }
+  *dd_out = best;
+  return obj;
+}
+
+// ObjectManager::FindCollision (object_manager.h:69-85): the hit nearest p1
+// over the scene's objects (kObjects), the hole (kHole) and the disc. Ties
+// keep the first one visited, in the order the reference's object map
+// visits them: the objects from last to first, then the hole, then the disc.
+template <typename R, bool kHole = true, bool kObjects = false>
 __device__ bool find_collision(const DevScene& s, V3<R> p1, V3<R> p2, Hit* out) {
   bool any = false;
   R best = R(0);
   V3<R> hp{};
   int which = BH_CLASS_MISS;
-  {
+  int obj = -1;
+  if (kObjects && s.n_objects > 0) {
+    obj = nearest_object<R>(s, p1, p2, &best, &hp);
+    if (obj >= 0) {
+      any = true;
+      which = BH_CLASS_OBJECT;
+    }
+  }
+  if (kHole) {
     const R rad = BH_S(R, s, r_h);
     const R d1 = length(p1), d2 = length(p2);
     if (!(d1 < rad && d2 < rad)) {
@@ -253,11 +384,15 @@ __device__ bool find_collision(const DevScene& s, V3<R> p1, V3<R> p2, Hit* out) 
       if (c > R(0)) {
         const R t = (R(1) / qq) * (-qp - sqrt(c));
         if (t > R(0) && t < R(1)) {
-          hp = p1 + Q * t;
-          const V3<R> d = p1 - hp;
-          best = dot(d, d);
-          any = true;
-          which = BH_CLASS_HORIZON;
+          const V3<R> h = p1 + Q * t;
+          const V3<R> d = p1 - h;
+          const R dd = dot(d, d);
+          if (!any || dd < best) {
+            best = dd;
+            hp = h;
+            any = true;
+            which = BH_CLASS_HORIZON;
+          }
         }
       }
     }
@@ -275,6 +410,7 @@ __device__ bool find_collision(const DevScene& s, V3<R> p1, V3<R> p2, Hit* out) 
         const V3<R> d = p1 - h;
         const R dd = dot(d, d);
         if (!any || dd < best) {
+          best = dd;
           hp = h;
           any = true;
           which = BH_CLASS_DISC;
@@ -284,12 +420,38 @@ __device__ bool find_collision(const DevScene& s, V3<R> p1, V3<R> p2, Hit* out) 
   }
   if (!any) return false;
   out->cls = which;
-  out->aux = 0.f;
-  out->bgra = which == BH_CLASS_DISC ? disc_color(s, hp) : make_uchar4(0, 0, 0, 255);
+  out->aux = which == BH_CLASS_OBJECT ? float(obj) : 0.f;
+  out->bgra = which == BH_CLASS_DISC     ? disc_color(s, hp)
+              : which == BH_CLASS_OBJECT ? object_color<R>(s.objects[obj], hp)
+                                         : make_uchar4(0, 0, 0, 255);
   return true;
 }
 
+// FLAT: the reference's flat-space RayTracer (ray_tracer.h:52-96) with
+// BasicLinearRayRecurrence (:17-33) as ray_tracer_test.cc:140-155 drives it:
+// from the focus toward the PixelVector point (REF raygen; PINHOLE: along
+// it), ten chords, the step scaled by 100 / |step|^2 when |step|^2 < 100.
+// e = focus - PixelVector point, so the first chord ends at F - e.
 template <typename R>
+__device__ Hit trace_flat(const DevScene& s, int x, int y) {
+  const R a = BH_S(R, s, half_w) - R(x), c = BH_S(R, s, half_h) - R(y);
+  const V3<R> e = BH_V(R, s, E0) + BH_V(R, s, vy) * a + BH_V(R, s, vz) * c;
+  V3<R> old = BH_V(R, s, F);
+  V3<R> pres = old - e;
+  V3<R> vec = pres - old;
+  const R d2 = dot(vec, vec);
+  if (d2 < R(100)) vec = vec * (R(100) / d2);
+  Hit hit = miss_hit();
+  for (int i = 0; i < 10; ++i) {
+    if (find_collision<R, false, true>(s, old, pres, &hit)) return hit;
+    const V3<R> next = pres + vec;
+    old = pres;
+    pres = next;
+  }
+  return hit;
+}
+
+template <typename R, bool kObjects = false>
 __device__ Hit trace_ref(const DevScene& s, int x, int y) {
   const PlaneRay<R> ray = make_ray<R>(s, x, y);
   const R M = BH_S(R, s, mass);
@@ -312,7 +474,7 @@ __device__ Hit trace_ref(const DevScene& s, int x, int y) {
     const R r = R(1) / u;
     const V3<R> cur = ray.yv * (r * cos(phi)) + ray.xv * (r * sin(phi));
     dphi_prev = dphi;
-    if (find_collision(s, prev, cur, &hit)) return hit;
+    if (find_collision<R, true, kObjects>(s, prev, cur, &hit)) return hit;
     prev = cur;
   }
   {
@@ -322,11 +484,11 @@ __device__ Hit trace_ref(const DevScene& s, int x, int y) {
     const R r = R(1) / u;
     const V3<R> cur = ray.yv * (r * cos(phi)) + ray.xv * (r * sin(phi));
     dphi_prev = dphi;
-    if (find_collision(s, prev, cur, &hit)) return hit;
+    if (find_collision<R, true, kObjects>(s, prev, cur, &hit)) return hit;
     prev = cur;
   }
   if (sol < R(0)) {
-    find_collision(s, prev, V3<R>{R(0), R(0), R(0)}, &hit);
+    find_collision<R, true, kObjects>(s, prev, V3<R>{R(0), R(0), R(0)}, &hit);
     return hit;
   }
   for (int i = 0; i < 19; ++i) {
@@ -335,7 +497,7 @@ __device__ Hit trace_ref(const DevScene& s, int x, int y) {
     phi += (dphi_prev + dphi) * du_h;
     const R r = R(1) / u;
     const V3<R> cur = ray.yv * (r * cos(phi)) + ray.xv * (r * sin(phi));
-    if (find_collision(s, prev, cur, &hit)) return hit;
+    if (find_collision<R, true, kObjects>(s, prev, cur, &hit)) return hit;
     dphi_prev = dphi;
     prev = cur;
   }
@@ -670,6 +832,71 @@ __device__ Hit trace_rk4(const DevScene& s, int x, int y, const Rk4Consts<R>& c,
   return finish_rk4<R>(s, st, c);
 }
 
+// Full trace in one precision R of a scene with objects: single RK4 steps,
+// each one's chord between the 3-D positions at its ends tested against the
+// objects (as the reference tests every chord of its integration). Within a
+// step the earlier event wins: a disc crossing at the fraction of the step's
+// angle where it lies, an object hit at its fraction of the chord. Horizon
+// and escape end the ray after the step's chord was tested.
+template <typename R>
+__device__ Hit trace_rk4_obj(const DevScene& s, int x, int y, const Rk4Consts<R>& c, int* steps) {
+  RayState<R> st;
+  init_rk4<R>(s, make_ray<R>(s, x, y), c.h, st);
+  const R M = BH_S(R, s, mass);
+  V3<R> prev = BH_V(R, s, F);
+  int k = 0;
+  while (st.status == kRunning) {
+    if (k >= c.kmax) {
+      st.status = kMaxSteps;
+      break;
+    }
+    // the step's disc crossing (if any) decided first, from the step's start
+    R f_disc = R(2);
+    if (k == st.kc) {
+      const R fr = (st.dcr - R(k) * c.h) / c.h;
+      if (cross_disc<R, false>(s, st, c.h)) f_disc = fmax(fr, R(0));
+    }
+    R xn = st.x, wn = st.w;
+    rk4_step<R>(xn, wn, c);
+    const R un = xn + R(1.0 / 3.0);
+    R f_obj = R(2);
+    Hit ho;
+    if (un > R(0)) {
+      const R rn = M / un;
+      R sp, cp;
+      sincos(R(k + 1) * c.h, &sp, &cp);
+      const V3<R> next = st.yv * (rn * cp) + st.xv * (rn * sp);
+      V3<R> hp;
+      R bd = R(0);
+      const int best = nearest_object<R>(s, prev, next, &bd, &hp);
+      if (best >= 0) {
+        const V3<R> ch = next - prev;
+        f_obj = sqrt(bd / dot(ch, ch));
+        ho.cls = BH_CLASS_OBJECT;
+        ho.aux = float(best);
+        ho.bgra = object_color<R>(s.objects[best], hp);
+      }
+      prev = next;
+    }
+    if (f_disc <= R(1) && f_disc <= f_obj) {
+      st.status = kDisc;
+      break;
+    }
+    if (f_obj <= R(1)) {
+      *steps = k + 1;
+      return ho;
+    }
+    st.xa = st.x;
+    st.wa = st.w;
+    st.x = xn;
+    st.w = wn;
+    st.k = ++k;
+    if (!inside(xn, c)) st.status = xn <= c.x_esc ? kEscape : kHorizon;
+  }
+  *steps = k;
+  return finish_rk4<R>(s, st, c);
+}
+
 // FP64 trace of a band ray (out of line: keeps FP64 register pressure away
 // from the FP32 callers).
 __device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
@@ -762,6 +989,33 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
       warp_add(&p.counters->band_rays, (unsigned long long)band_ray);
       warp_add(&p.counters->band_steps, band_ray ? (unsigned long long)steps : 0ull);
     }
+  }
+}
+
+// GRID schedule for the FLAT integrator and for scenes with objects (FP32 or
+// FP64): a kernel of its own, so that the object code does not raise the
+// register count of grid_kernel.
+__global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
+  const DevScene& s = p.scenes[blockIdx.z];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= s.width || y >= s.height) return;
+  Hit h;
+  int steps = 0;
+  const bool fp64 = p.precision == BH_PRECISION_FP64;
+  if (p.integrator == BH_INTEGRATOR_FLAT) {
+    h = fp64 ? trace_flat<double>(s, x, y) : trace_flat<float>(s, x, y);
+  } else if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+    h = fp64 ? trace_ref<double, true>(s, x, y) : trace_ref<float, true>(s, x, y);
+  } else if (s.n_objects > 0) {
+    h = fp64 ? trace_rk4_obj<double>(s, x, y, p.c64, &steps) : trace_rk4_obj<float>(s, x, y, p.c32, &steps);
+  } else {
+    h = fp64 ? trace_rk4<double, false>(s, x, y, p.c64, &steps) : trace_rk4<float, false>(s, x, y, p.c32, &steps);
+  }
+  store_hit(s, p.format, x, y, h);
+  if (p.counters) {
+    warp_add(&p.counters->steps, (unsigned long long)steps);
+    warp_add(&p.counters->rays, 1ull);
   }
 }
 
@@ -1071,7 +1325,7 @@ __global__ void fp64_probe_kernel(double* sink, int iters) {
 // ---------------------------------------------------------------------------
 // launchers
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
-                        int block_x, int block_y, cudaStream_t stream) {
+                        int block_x, int block_y, cudaStream_t stream, bool objects) {
   int max_w = 0, max_h = 0;
   for (int i = 0; i < p.n_scenes; ++i) {
     max_w = scene_w[i] > max_w ? scene_w[i] : max_w;
@@ -1079,7 +1333,8 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
   }
   const dim3 block(block_x, block_y, 1);
   const dim3 grid((max_w + block_x - 1) / block_x, (max_h + block_y - 1) / block_y, p.n_scenes);
-  grid_kernel<<<grid, block, 0, stream>>>(p);
+  if (objects) grid_objects_kernel<<<grid, block, 0, stream>>>(p);
+  else grid_kernel<<<grid, block, 0, stream>>>(p);
   return cudaGetLastError();
 }
 

@@ -80,13 +80,15 @@ class Renderer:
 
     def c_scenes(self, scenes: list[Scene]):
         for s in scenes:
-            if s.disc is not None:
-                self.texture_id(s.disc.texture)
-            if s.background is not None:
-                self.texture_id(s.background)
+            for t in s.textures():
+                self.texture_id(t)
         arr = (capi.Scene * len(scenes))()
+        keep = []
         for i, s in enumerate(scenes):
-            arr[i] = s.to_c(self._tex_ids)
+            c = s.to_c(self._tex_ids)
+            arr[i] = c
+            keep.append(c._keep)
+        arr._keep = keep  # the object tables the scenes point at
         return arr
 
     # -- rendering ----------------------------------------------------------------

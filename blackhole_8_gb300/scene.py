@@ -22,6 +22,7 @@ machine and numpy version.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 from dataclasses import dataclass, field
 
@@ -258,6 +259,74 @@ class Annulus(Object):
         return d
 
 
+class Rectangle(Object):
+    """Rectangle<T> (vector_object.h:80-183): corners p1..p4 follow the
+    default (0,0,0) vertex; drawn by Rectangle::color from its texture."""
+
+    def __init__(self, p1, p2, p3, p4):
+        super().__init__(((0.0, 0.0, 0.0), p1, p2, p3, p4))
+        self.construction = tuple(np.array(p, dtype=np.float64) for p in (p1, p2, p3, p4))
+        self.texture: Texture | None = None
+
+    def SetTexture(self, texture: "Texture") -> None:
+        if texture is None or texture.empty():
+            raise ValueError("empty texture (the reference terminates here, material.h:30-33)")
+        self.texture = texture
+
+    def to_c(self, texture_ids: dict) -> capi.Object:
+        o = capi.Object()
+        o.type = capi.OBJECT_RECTANGLE
+        o.texture = texture_ids[id(self.texture)] if self.texture is not None else -1
+        for k in range(4):
+            o.v[k][:] = list(self._v[k + 1])
+        return o
+
+
+class Triangle(Object):
+    """Triangle<T> (vector_object.h:18-77): vertices v1..v3 follow the default
+    (0,0,0) vertex; it has no colour of its own (black, material.h:54)."""
+
+    def __init__(self, v1, v2, v3):
+        super().__init__(((0.0, 0.0, 0.0), v1, v2, v3))
+
+    def to_c(self, texture_ids: dict) -> capi.Object:
+        o = capi.Object()
+        o.type = capi.OBJECT_TRIANGLE
+        o.texture = -1
+        for k in range(3):
+            o.v[k][:] = list(self._v[k + 1])
+        return o
+
+
+class ChessPattern2D:
+    """ChessPattern2D<T> (pattern.h:14-50): black and white cells of
+    `pattern_size`."""
+
+    def __init__(self, pattern_size: float = 1):
+        self.pattern_size = float(pattern_size)
+
+
+class InfinitePlane(Object):
+    """InfinitePlane<T> (vector_object.h:187-238): the plane through
+    position() normal to vector_z(), coloured by a ChessPattern2D (or black)."""
+
+    def __init__(self, p, pattern: ChessPattern2D | None = None):
+        super().__init__((p,))
+        self.construction = (np.array(p, dtype=np.float64),)
+        self.pattern = pattern
+
+    def to_c(self, texture_ids: dict) -> capi.Object:
+        o = capi.Object()
+        o.type = capi.OBJECT_PLANE
+        o.texture = -1
+        o.v[0][:] = list(self._v[0])
+        o.axis_x[:] = list(self._vx)
+        o.axis_y[:] = list(self._vy)
+        o.axis_z[:] = list(self._vz)
+        o.pattern_size = self.pattern.pattern_size if self.pattern is not None else 0.0
+        return o
+
+
 class Texture:
     """Host texture (H, W, C) uint8 with a channel layout (capi.TEXEL_*)."""
 
@@ -301,8 +370,17 @@ class Scene:
     disc: Annulus | None = None
     background: Texture | None = None
     meta: dict = field(default_factory=dict)
+    objects: list = field(default_factory=list)  # Rectangle / Triangle / InfinitePlane, in table order
+
+    def textures(self) -> list:
+        """Every texture the scene draws with."""
+        out = [t for t in (self.disc.texture if self.disc is not None else None, self.background) if t is not None]
+        out += [o.texture for o in self.objects if getattr(o, "texture", None) is not None]
+        return out
 
     def to_c(self, texture_ids: dict) -> capi.Scene:
+        """The C scene; its object table lives in the returned struct's
+        `_keep` attribute, which the caller keeps alive while the C ABI reads it."""
         s = capi.Scene()
         s.camera = self.camera.to_c()
         s.hole = self.hole.to_c()
@@ -312,6 +390,12 @@ class Scene:
             s.disc.enabled = 0
             s.disc.texture = -1
         s.background = texture_ids[id(self.background)] if self.background is not None else -1
+        s._keep = None
+        if self.objects:
+            arr = (capi.Object * len(self.objects))(*[o.to_c(texture_ids) for o in self.objects])
+            s.objects = C.cast(arr, C.POINTER(capi.Object))
+            s.n_objects = len(self.objects)
+            s._keep = arr
         return s
 
 
@@ -449,6 +533,56 @@ def single_scene(width: int = 640, height: int = 360, seed: int = 0) -> Scene:
     cam = aimed_camera(width, height, math.radians(60), 20.0, math.radians(80))
     return Scene(cam, StaticBlackhole((0.0, 0.0, 0.0), 1.0), equatorial_disc(6.0, 20.0, disc_tex), bg,
                  {"workload": f"single {width}x{height}"})
+
+
+def panel_texture(seed: int, width: int = 160, height: int = 120) -> Texture:
+    """A hash-noise BGR8 picture for a Rectangle (no black texels)."""
+    def make():
+        t = value_noise_background(seed, width, height, octaves=2, base_cells=8).bgra()[..., :3].copy()
+        t[t.sum(-1) == 0] = 1
+        return Texture(t, capi.TEXEL_BGR8)
+    return _cached(("panel", seed, width, height), make)
+
+
+def flat_demo_scene(width: int = 800, height: int = 450, seed: int = 0) -> Scene:
+    """The reference's flat RayTracer scene (ray_tracer_test.cc:50-98):
+    Camera(W, H, pi/2) moved to (-400, 120, 100), RotateY(-pi/24),
+    RotateZ(pi/12); three textured Rectangles (hash pictures stand in for
+    the photos) and an InfinitePlane through the origin with
+    ChessPattern2D{10}. The hole takes no part in the FLAT integrator."""
+    cam = Camera(width, height, math.pi / 2)
+    cam.MoveTo(-400, 120, 100)
+    cam.RotateY(-math.pi / 24)
+    cam.RotateZ(math.pi / 12)
+    rects = [
+        ((100, 120, 100), (100, 0, 100), (100, 0, 0), (100, 120, 0)),
+        ((100, 0, 150), (100, -100, 150), (100, -100, 0), (100, 0, 0)),
+        ((-100, 50, 100), (-100, -50, 100), (-100, -50, 0), (-100, 50, 0)),
+    ]
+    objects = []
+    for k, corners in enumerate(rects):
+        r = Rectangle(*corners)
+        r.SetTexture(panel_texture(seed + 10 + k))
+        objects.append(r)
+    objects.append(InfinitePlane((0.0, 0.0, 0.0), ChessPattern2D(10)))
+    return Scene(cam, StaticBlackhole((0.0, 0.0, 0.0), 1.0), None, None,
+                 {"workload": f"flat demo {width}x{height}"}, objects)
+
+
+def objects_scene(width: int = 640, height: int = 360, seed: int = 0) -> Scene:
+    """The single-scene workload with ordinary objects inside the camera's
+    radius: a chess plane 6 M below the disc (ChessPattern2D{2}), a textured
+    panel standing behind the hole at x = 12 M and one beside it at
+    y = -10 M. The disc takes the reference's planar map."""
+    sc = single_scene(width, height, seed)
+    sc.disc.mapping = capi.DISC_MAP_REF_PLANAR
+    back = Rectangle((12, 8, 8), (12, -8, 8), (12, -8, -4), (12, 8, -4))
+    back.SetTexture(panel_texture(seed + 20))
+    side = Rectangle((-8, -10, 6), (8, -10, 6), (8, -10, -2), (-8, -10, -2))
+    side.SetTexture(panel_texture(seed + 21))
+    sc.objects = [InfinitePlane((0.0, 0.0, -6.0), ChessPattern2D(2)), back, side]
+    sc.meta = {"workload": f"objects {width}x{height}"}
+    return sc
 
 
 def flythrough(frames: int = 120, width: int = 1920, height: int = 1080, seed: int = 0) -> list[Scene]:

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define BH_ABI_VERSION 1
+#define BH_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 enum {
@@ -53,8 +53,14 @@ enum {
 /* Integrator. REF_TRAPEZOID is the reference's own scheme: dphi/du = 1/sqrt(G)
  * by a 20+20-segment trapezoid rule in u with straight-chord collision tests
  * (blackhole_solution_test.cc:185-296). RK4 integrates u'' = -u + 3 M u^2 in
- * phi with a fixed step and exact horizon / escape / disc-plane events. */
-enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1 };
+ * phi with a fixed step and exact horizon / escape / disc-plane events; the
+ * scene's objects are tested on the chord of every step. FLAT is the
+ * reference's flat-space RayTracer (ray_tracer.h:52-96 with
+ * BasicLinearRayRecurrence, driven as in ray_tracer_test.cc:140-155): ten
+ * straight chords from the focus through the PixelVector point, the step
+ * scaled by 100 / |step|^2 when |step|^2 < 100, tested against the objects
+ * and the disc; the hole does not bend or stop it (GRID schedule only). */
+enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1, BH_INTEGRATOR_FLAT = 2 };
 
 /* Arithmetic. MIXED (RK4 only): FP32 bulk, FP64 for rays whose impact
  * parameter lies within `band` of 3*sqrt(3)*M, FP64 disc-crossing refinement. */
@@ -84,8 +90,44 @@ enum { BH_TEXEL_BGR8 = 0, BH_TEXEL_RGB8 = 1, BH_TEXEL_BGRA8 = 2, BH_TEXEL_RGBA8 
  * second persistent pass. */
 enum { BH_SCHEDULE_GRID = 0, BH_SCHEDULE_PERSISTENT = 1 };
 
-/* Per-pixel hit classes written to bh_frame.hit_class. */
-enum { BH_CLASS_MISS = 0, BH_CLASS_HORIZON = 1, BH_CLASS_DISC = 2, BH_CLASS_MAXSTEPS = 3 };
+/* Per-pixel hit classes written to bh_frame.hit_class. OBJECT: one of the
+ * scene's bh_objects (aux holds its index). */
+enum { BH_CLASS_MISS = 0, BH_CLASS_HORIZON = 1, BH_CLASS_DISC = 2, BH_CLASS_MAXSTEPS = 3, BH_CLASS_OBJECT = 4 };
+
+/* Ordinary objects (object/vector_object.h, object/pattern.h). Each is drawn
+ * where a chord of the ray crosses it, the hit nearest the chord's start
+ * first, as ObjectManager::FindCollision (object_manager.h:69-85). On exact
+ * distance ties the reference keeps the first object its map visits; with
+ * the disc inserted first, the hole second and the objects after them in
+ * table order, libstdc++ visits the objects from last to first, then the
+ * hole, then the disc, and so does the tracer.
+ * RECTANGLE: Rectangle<T> (vector_object.h:80-183) with vertex()[1..4] =
+ *   v[0..3]: the chord crosses the plane of v1, v2, v4 inside the quad;
+ *   colour by Rectangle::color from `texture` (nearest texel, truncating
+ *   casts; indices clamped to the texture where the reference reads
+ *   outside it), or black with texture -1.
+ * TRIANGLE: Triangle<T> (vector_object.h:18-77), Moller-Trumbore on
+ *   vertex()[1..3] = v[0..2] with epsilon 10 * machine epsilon of the
+ *   arithmetic; drawn black (it has no colour of its own, material.h:54).
+ * PLANE: InfinitePlane<T> (vector_object.h:187-238) through position() =
+ *   v[0] with unit axes axis_x, axis_y and normal axis_z (Object<T> axes);
+ *   colour ChessPattern2D<T>{pattern_size} (pattern.h:14-46) at the plane
+ *   coordinates InfinitePlane::color derives from the hit's world x and y,
+ *   or black with pattern_size <= 0. */
+enum { BH_OBJECT_RECTANGLE = 1, BH_OBJECT_TRIANGLE = 2, BH_OBJECT_PLANE = 3 };
+
+typedef struct bh_object {
+  int32_t type;        /* BH_OBJECT_* */
+  int32_t texture;     /* RECTANGLE: texture id from bh_texture_create, or -1 */
+  double v[4][3];      /* vertices (world coordinates), see above */
+  double axis_x[3];    /* PLANE: vector_x(), vector_y(), vector_z() */
+  double axis_y[3];
+  double axis_z[3];
+  double pattern_size; /* PLANE: ChessPattern2D pattern size */
+} bh_object;
+
+/* Objects per scene accepted by the render calls. */
+#define BH_MAX_OBJECTS 64
 
 /* ---- scene ------------------------------------------------------------------ */
 /* Camera<T> state (camera.h:21-71 on Object<T>, object/object.h:23-118). */
@@ -127,16 +169,21 @@ typedef struct bh_scene {
   int32_t background;  /* equirectangular texture id, or -1: escaped rays stay
                           black as in the reference (screen is zeroed,
                           blackhole_solution_test.cc:140) */
-  int32_t reserved;
+  int32_t n_objects;   /* entries of `objects` (0..BH_MAX_OBJECTS) */
+  const bh_object* objects; /* host memory, read during the call; NULL when
+                          n_objects is 0. Objects need the GRID schedule and
+                          FP32 or FP64 (not MIXED), and no differentiable
+                          render. */
 } bh_scene;
 
 /* One output frame; width and height come from the scene's camera. */
 typedef struct bh_frame {
   void* pixels;        /* width*height*bytes_per_pixel(format), row-major */
   uint8_t* hit_class;  /* optional (NULL): width*height BH_CLASS_* */
-  float* aux;          /* optional (NULL): width*height. RK4 only: deflection
+  float* aux;          /* optional (NULL): width*height. RK4: deflection
                           angle (rad) of escaped rays, hit radius (units of M)
-                          of disc hits, 0 otherwise */
+                          of disc hits; RK4 and FLAT: the object's index of
+                          object hits; 0 otherwise (not REF_TRAPEZOID) */
 } bh_frame;
 
 typedef struct bh_render_options {
@@ -272,7 +319,8 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
  * library only pre-allocated device buffers -- and so cannot use bh_render or
  * bh_render_device, whose contexts grow their buffers with cudaMalloc.
  * Textures (BGRA8, caller-owned device memory, indexed by the scenes'
- * texture ids) and frames are in device memory; scenes are on the host. The
+ * texture ids) and frames are in device memory; scenes are on the host and
+ * carry no objects (n_objects 0; the FLAT integrator is not offered). The
  * library's own scratch (counters, scene records, the FP64 band list) lives
  * in one fixed device array of about 34 MiB that every device loading the
  * library holds until exit; calls are limited to BH_NOALLOC_MAX_SCENES scenes

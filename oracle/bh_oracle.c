@@ -27,6 +27,20 @@
  *     escape at u = M / r_escape (Hermite-refined), disc-plane crossings at
  *     phi = phi_node + j*pi (partial RK4 step) and the step cap.
  *
+ *   orc_render_flat -- the reference's flat-space RayTracer (ray_tracer.h:
+ *     52-96, BasicLinearRayRecurrence :17-33) as ray_tracer_test.cc:140-155
+ *     drives it: ten chords from the focus through the PixelVector point,
+ *     the step scaled by 100 / |step|^2 when |step|^2 < 100.
+ *
+ *   Ordinary objects (bh_object) take part in every chord test of modes A
+ *   and flat, and of each RK4 step of mode B: Rectangle::Collide / color
+ *   (vector_object.h:107-180), Triangle::Collide (:39-71, black),
+ *   InfinitePlane::Collide / color (:210-232) with ChessPattern2D
+ *   (pattern.h:23-46). FindCollision keeps the first object visited on exact
+ *   ties, visiting the objects from last to first, then the hole, then the
+ *   disc (the reference's map order with the disc and the hole inserted
+ *   first).
+ *
  * Outputs per pixel: BGRA bytes, hit class, an aux value (deflection angle of
  * escaped rays, hit radius / M of disc hits), margins to the nearest texel
  * edge and disc edge (used by the tests to separate boundary pixels), b / M
@@ -126,6 +140,9 @@ typedef struct {
   double r_in, r_out;
   orc_texture disc_tex, bg_tex;
   int has_bg;
+  int n_obj;
+  const bh_object* obj;
+  const orc_texture* obj_tex; /* one per object (NULL bgra: none), or NULL */
 } view;
 
 static void make_view(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* bg_tex, view* v) {
@@ -155,6 +172,8 @@ static void make_view(const bh_scene* s, const orc_texture* disc_tex, const orc_
   }
   v->has_bg = s->background >= 0 && bg_tex && bg_tex->bgra;
   if (v->has_bg) v->bg_tex = *bg_tex;
+  v->n_obj = s->n_objects;
+  v->obj = s->objects;
 }
 
 /* Camera::focus_vector / PixelVector(x, y, fv), camera.h:55-63 */
@@ -272,24 +291,164 @@ static int collide_disc(const view* v, vec3 q1, vec3 q2, vec3* hit) {
   return 1;
 }
 
-/* ObjectManager::FindCollision: nearest to p1; the hole is visited first and
- * keeps exact ties. Returns the class, writes the colour. */
-static int find_collision(const view* v, vec3 p1, vec3 p2, uint8_t out[4]) {
-  vec3 h1, h2;
-  int got1 = collide_hole(v, p1, p2, &h1);
-  int got2 = v->disc_on && collide_disc(v, p1, p2, &h2);
-  if (!got1 && !got2) return BH_CLASS_MISS;
-  int use_disc = got2;
-  if (got1 && got2) {
-    vec3 a = sub(p1, h1), b = sub(p1, h2);
-    use_disc = dot(b, b) < dot(a, a);
+/* Rectangle::Collide, vector_object.h:107-127 */
+static int collide_rect(const bh_object* o, vec3 aa, vec3 bb, vec3* hit) {
+  vec3 p0 = v3a(o->v[0]);
+  vec3 p1 = sub(v3a(o->v[1]), p0);
+  vec3 p3 = sub(v3a(o->v[3]), p0);
+  vec3 n = normalize(cross(p1, p3));
+  vec3 Q1 = sub(aa, p0), Q2 = sub(bb, p0);
+  double q1 = dot(n, Q1), q2 = dot(n, Q2);
+  if (q1 * q2 >= 0) return 0;
+  double a1 = fabs(q1), a2 = fabs(q2), d = a1 + a2;
+  vec3 s = add(scale(Q1, a2), scale(Q2, a1));
+  vec3 Q = v3(s.x / d, s.y / d, s.z / d);
+  if (dot(p1, Q) > 0 && dot(p1, p1) > dot(p1, Q) && dot(p3, Q) > 0 && dot(p3, p3) > dot(p3, Q)) {
+    *hit = add(Q, p0);
+    return 1;
   }
-  if (use_disc) {
-    color_disc(v, h2, out, NULL);
-    return BH_CLASS_DISC;
+  return 0;
+}
+
+/* Triangle::Collide, vector_object.h:39-71 (Moller-Trumbore; no upper bound
+ * on t, as in the reference) */
+static int collide_tri(const bh_object* o, vec3 p1, vec3 p2, vec3* hit) {
+  const double ep = 2.220446049250313e-16 * 10;
+  vec3 rv = sub(p2, p1);
+  vec3 v0 = v3a(o->v[0]);
+  vec3 e1 = sub(v3a(o->v[1]), v0), e2 = sub(v3a(o->v[2]), v0);
+  vec3 h = cross(rv, e2);
+  double a = dot(e1, h);
+  if (-ep < a && a < ep) return 0;
+  double f = 1.0 / a;
+  vec3 s = sub(p1, v0);
+  double u = f * dot(s, h);
+  if (u < 0 || u > 1) return 0;
+  vec3 q = cross(s, e1);
+  double w = f * dot(rv, q);
+  if (w < 0 || u + w > 1) return 0;
+  double t = f * dot(e2, q);
+  if (t <= ep) return 0;
+  *hit = add(p1, scale(rv, t));
+  return 1;
+}
+
+/* InfinitePlane::Collide, vector_object.h:210-225 */
+static int collide_plane(const bh_object* o, vec3 p1, vec3 p2, vec3* hit) {
+  const double* z = o->axis_z;
+  const double* pos = o->v[0];
+  double t1 = z[0] * (p1.x - pos[0]) + z[1] * (p1.y - pos[1]) + z[2] * (p1.z - pos[2]);
+  double t2 = z[0] * (p2.x - pos[0]) + z[1] * (p2.y - pos[1]) + z[2] * (p2.z - pos[2]);
+  if (t1 * t2 > 0) return 0;
+  double d1 = fabs(t1), d2 = fabs(t2), d = d1 + d2;
+  vec3 s = add(scale(p1, d2), scale(p2, d1));
+  *hit = v3(s.x / d, s.y / d, s.z / d);
+  return 1;
+}
+
+static int collide_object(const bh_object* o, vec3 p1, vec3 p2, vec3* hit) {
+  if (o->type == BH_OBJECT_RECTANGLE) return collide_rect(o, p1, p2, hit);
+  if (o->type == BH_OBJECT_TRIANGLE) return collide_tri(o, p1, p2, hit);
+  return collide_plane(o, p1, p2, hit);
+}
+
+/* ChessPattern2D<T>{size}, pattern.h:23-46 ((int) casts pinned) */
+static void chess(double size, double x, double y, uint8_t out[4]) {
+  int m = trunc_int(size * 2);
+  int white = 0;
+  if (m != 0) {
+    double bx = fabs(x), by = fabs(y);
+    double x2 = bx - (double)(trunc_int(bx) / m) * (size * 2);
+    double y2 = by - (double)(trunc_int(by) / m) * (size * 2);
+    int in = (x2 <= size && y2 <= size) || (size <= x2 && size <= y2);
+    white = x * y > 0 ? in : !in;
+  }
+  out[0] = out[1] = out[2] = white ? 255 : 0;
+}
+
+/* Rectangle::color (vector_object.h:163-180), InfinitePlane::color (:227-232),
+ * Material::color for triangles (black) */
+static void color_object(const view* v, int i, vec3 p, uint8_t out[4]) {
+  const bh_object* o = &v->obj[i];
+  out[0] = out[1] = out[2] = 0;
+  if (o->type == BH_OBJECT_RECTANGLE) {
+    const orc_texture* t = v->obj_tex ? &v->obj_tex[i] : NULL;
+    if (!t || !t->bgra) return;
+    vec3 v1 = v3a(o->v[0]);
+    vec3 s1 = sub(v3a(o->v[1]), v1), s2 = sub(v3a(o->v[3]), v1);
+    vec3 q = sub(p, v1);
+    double r = sqrt(dot(q, q));
+    double theta = acos(dot(s1, q) / (sqrt(dot(s1, s1)) * r));
+    theta = isnan(theta) ? 0 : theta;
+    int px_w = trunc_int((r * cos(theta) / sqrt(dot(s1, s1))) * t->width);
+    int px_h = trunc_int((r * sin(theta) / sqrt(dot(s2, s2))) * t->height);
+    read_texel(t, (long long)px_h * t->width + px_w, out);
+  } else if (o->type == BH_OBJECT_PLANE && o->pattern_size > 0) {
+    const double* vx = o->axis_x;
+    const double* vy = o->axis_y;
+    double b = (vx[0] * p.y - vx[1] * p.x) / (vx[0] * vy[1] - vx[1] * vy[0]);
+    double a = (p.x - b * vy[0]) / vx[0];
+    chess(o->pattern_size, a, b, out);
+  }
+}
+
+/* Nearest object hit to p1 on the chord (objects visited from last to first,
+ * the first keeps ties); -1 when none. */
+static int nearest_object(const view* v, vec3 p1, vec3 p2, double* dd_out, vec3* hit) {
+  int obj = -1;
+  double best = 0;
+  for (int i = v->n_obj - 1; i >= 0; --i) {
+    vec3 h;
+    if (collide_object(&v->obj[i], p1, p2, &h)) {
+      vec3 d = sub(p1, h);
+      double dd = dot(d, d);
+      if (obj < 0 || dd < best) {
+        obj = i;
+        best = dd;
+        *hit = h;
+      }
+    }
+  }
+  *dd_out = best;
+  return obj;
+}
+
+/* ObjectManager::FindCollision: nearest to p1 over the objects, the hole
+ * (with_hole) and the disc; returns the class, writes the colour and, for an
+ * object, its index. */
+static int find_collision_objects(const view* v, vec3 p1, vec3 p2, int with_hole, uint8_t out[4], int* obj_out) {
+  int cls = BH_CLASS_MISS, obj = -1;
+  double best = 0;
+  vec3 hp = v3(0, 0, 0), h;
+  obj = nearest_object(v, p1, p2, &best, &hp);
+  if (obj >= 0) cls = BH_CLASS_OBJECT;
+  if (with_hole && collide_hole(v, p1, p2, &h)) {
+    vec3 d = sub(p1, h);
+    double dd = dot(d, d);
+    if (cls == BH_CLASS_MISS || dd < best) {
+      cls = BH_CLASS_HORIZON;
+      best = dd;
+      hp = h;
+    }
+  }
+  if (v->disc_on && collide_disc(v, p1, p2, &h)) {
+    vec3 d = sub(p1, h);
+    double dd = dot(d, d);
+    if (cls == BH_CLASS_MISS || dd < best) {
+      cls = BH_CLASS_DISC;
+      best = dd;
+      hp = h;
+    }
   }
   out[0] = out[1] = out[2] = 0;
-  return BH_CLASS_HORIZON;
+  if (cls == BH_CLASS_DISC) color_disc(v, hp, out, NULL);
+  if (cls == BH_CLASS_OBJECT) color_object(v, obj, hp, out);
+  if (obj_out) *obj_out = cls == BH_CLASS_OBJECT ? obj : -1;
+  return cls;
+}
+
+static int find_collision(const view* v, vec3 p1, vec3 p2, uint8_t out[4]) {
+  return find_collision_objects(v, p1, p2, 1, out, NULL);
 }
 
 /* StaticBlackhole::G, InvSqrtG, SolveG (blackhole_solution.h:27-53) */
@@ -486,6 +645,137 @@ static void rk4_pixel(const view* v, const orc_rk4_opts* o, int x, int y, rk4_re
   res->steps = o->max_steps;
 }
 
+/* Mode B with objects: each RK4 step's chord between the positions at its
+ * ends is tested against the objects; within a step the earlier event wins,
+ * a disc crossing at its fraction of the step's angle, an object hit at its
+ * fraction of the chord. */
+static void rk4_pixel_obj(const view* v, const orc_rk4_opts* o, int x, int y, rk4_result* res) {
+  plane p;
+  reduce(v, x, y, &p);
+  memset(res, 0, sizeof(*res));
+  res->bgra[3] = 255;
+  res->margin_tex = 1.0;
+  res->margin_r = 1e30;
+  const double M = v->M, h = o->step;
+  const double b = p.Fc.z, bm = b / M;
+  res->b_over_m = bm;
+  const double r0 = sqrt(dot(p.Fc, p.Fc));
+  double u = M / r0;
+  const double phi0 = atan2(p.Fc.z, p.Fc.y);
+  if (!(bm > 1e-6)) {
+    res->cls = BH_CLASS_HORIZON;
+    return;
+  }
+  double w = copysign(sqrt(fmax(1.0 / (bm * bm) - u * u * (1.0 - 2.0 * u), 0.0)), p.Fc.y);
+  const double u_esc = 1.0 / o->r_escape;
+  long long kc = -1;
+  double dcr = 0;
+  if (v->disc_on) {
+    double A = dot(v->dnorm, p.yv), B = dot(v->dnorm, p.xv);
+    if (A * A + B * B > 1e-24) {
+      dcr = fmod(atan2(B, A) + ORC_PI / 2 - phi0, ORC_PI);
+      if (dcr <= 0) dcr += ORC_PI;
+      kc = (long long)floor(dcr / h);
+    }
+  }
+  vec3 prev = v->focus;
+  for (int k = 0; k < o->max_steps; ++k) {
+    double f_disc = 2, rc_hit = 0;
+    if (k == kc) {
+      double uc = u, wc = w;
+      rk4(&uc, &wc, dcr - kc * h);
+      double rc = 1.0 / uc;
+      if (uc < 0.5 && rc * M >= v->r_in && rc * M <= v->r_out) {
+        double fr = (dcr - kc * h) / h;
+        f_disc = fr < 0 ? 0 : fr;
+        rc_hit = rc;
+      } else {
+        dcr += ORC_PI;
+        kc = (long long)floor(dcr / h);
+      }
+    }
+    double ua = u, wa = w, un = u, wn = w;
+    rk4(&un, &wn, h);
+    double f_obj = 2;
+    int obj = -1;
+    vec3 ohit = v3(0, 0, 0);
+    if (un > 0) {
+      vec3 next = back_project(v, &p, M / un, phi0 + (k + 1) * h);
+      double dd = 0;
+      obj = nearest_object(v, prev, next, &dd, &ohit);
+      if (obj >= 0) {
+        vec3 ch = sub(next, prev);
+        f_obj = sqrt(dd / dot(ch, ch));
+      }
+      prev = next;
+    }
+    if (f_disc <= 1 && f_disc <= f_obj) {
+      vec3 hit = back_project(v, &p, rc_hit * M, phi0 + dcr);
+      res->cls = BH_CLASS_DISC;
+      res->aux = rc_hit;
+      double dr1 = rc_hit - v->r_in / M, dr2 = v->r_out / M - rc_hit;
+      res->margin_r = dr1 < dr2 ? dr1 : dr2;
+      color_disc(v, hit, res->bgra, &res->margin_tex);
+      res->steps = k;
+      return;
+    }
+    if (f_obj <= 1) {
+      res->cls = BH_CLASS_OBJECT;
+      res->aux = obj;
+      color_object(v, obj, ohit, res->bgra);
+      res->steps = k + 1;
+      return;
+    }
+    u = un;
+    w = wn;
+    if (!(u < 0.5)) {
+      res->cls = BH_CLASS_HORIZON;
+      res->steps = k + 1;
+      return;
+    }
+    if (u <= u_esc) {
+      double t = (ua - u_esc) / (ua - u), pp, dp;
+      for (int i = 0; i < 8; ++i) {
+        hermite(ua, h * wa, u, h * w, t, &pp, &dp);
+        t -= (pp - u_esc) / dp;
+        if (t < 0) t = 0;
+        if (t > 1) t = 1;
+      }
+      hermite(ua, h * wa, u, h * w, t, &pp, &dp);
+      double we = dp / h;
+      double psi = phi0 + (k + t) * h + atan2(u_esc, -we);
+      res->cls = BH_CLASS_MISS;
+      res->aux = psi - ORC_PI;
+      res->steps = k + 1;
+      if (v->has_bg) {
+        vec3 d = add(scale(p.yv, cos(psi)), scale(p.xv, sin(psi)));
+        color_background(v, d, res->bgra, &res->margin_tex);
+      }
+      return;
+    }
+  }
+  res->cls = BH_CLASS_MAXSTEPS;
+  res->steps = o->max_steps;
+}
+
+/* The flat RayTracer (REF ray generation): ten chords, then a miss. */
+static int flat_pixel(const view* v, int x, int y, uint8_t out[4], int* obj) {
+  vec3 fv = scale(v->vx, v->focus_len);
+  vec3 old = v->focus;
+  vec3 pres = pixel_vector(v, x, y, fv);
+  vec3 vec = sub(pres, old);
+  double d2 = dot(vec, vec);
+  if (d2 < 100) vec = scale(vec, 100.0 / d2);
+  for (int i = 0; i < 10; ++i) {
+    int cls = find_collision_objects(v, old, pres, 0, out, obj);
+    if (cls != BH_CLASS_MISS) return cls;
+    vec3 next = add(pres, vec);
+    old = pres;
+    pres = next;
+  }
+  return BH_CLASS_MISS;
+}
+
 /* ------------------------------------------------------------------------- */
 static void set_threads(int nthreads) {
 #ifdef _OPENMP
@@ -497,10 +787,11 @@ static void set_threads(int nthreads) {
 
 /* Mode A over the whole image (pixels == NULL) or a list of npix pixels
  * given as (x, y) pairs. Outputs are indexed like the pixels. */
-int orc_render_ref(const bh_scene* s, const orc_texture* disc_tex, const int32_t* pixels, int64_t npix,
-                   const orc_outputs* out, int nthreads) {
+int orc_render_ref(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* obj_tex,
+                   const int32_t* pixels, int64_t npix, const orc_outputs* out, int nthreads) {
   view v;
   make_view(s, disc_tex, NULL, &v);
+  v.obj_tex = obj_tex;
   const int64_t n = pixels ? npix : (int64_t)v.W * v.H;
   set_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 64)
@@ -517,10 +808,11 @@ int orc_render_ref(const bh_scene* s, const orc_texture* disc_tex, const int32_t
 }
 
 int orc_render_rk4(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* bg_tex,
-                   const orc_rk4_opts* o, const int32_t* pixels, int64_t npix, const orc_outputs* out,
-                   int nthreads) {
+                   const orc_texture* obj_tex, const orc_rk4_opts* o, const int32_t* pixels, int64_t npix,
+                   const orc_outputs* out, int nthreads) {
   view v;
   make_view(s, disc_tex, bg_tex, &v);
+  v.obj_tex = obj_tex;
   const int64_t n = pixels ? npix : (int64_t)v.W * v.H;
   set_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 16)
@@ -528,7 +820,8 @@ int orc_render_rk4(const bh_scene* s, const orc_texture* disc_tex, const orc_tex
     int x = pixels ? pixels[2 * i] : (int)(i % v.W);
     int y = pixels ? pixels[2 * i + 1] : (int)(i / v.W);
     rk4_result r;
-    rk4_pixel(&v, o, x, y, &r);
+    if (v.n_obj > 0) rk4_pixel_obj(&v, o, x, y, &r);
+    else rk4_pixel(&v, o, x, y, &r);
     if (out->bgra) memcpy(out->bgra + 4 * i, r.bgra, 4);
     if (out->cls) out->cls[i] = (uint8_t)r.cls;
     if (out->aux) out->aux[i] = r.aux;
@@ -536,6 +829,30 @@ int orc_render_rk4(const bh_scene* s, const orc_texture* disc_tex, const orc_tex
     if (out->margin_r) out->margin_r[i] = r.margin_r;
     if (out->b_over_m) out->b_over_m[i] = r.b_over_m;
     if (out->steps) out->steps[i] = r.steps;
+  }
+  return 0;
+}
+
+/* Flat mode over the whole image or a pixel list; aux receives the object
+ * index of object hits. */
+int orc_render_flat(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* obj_tex,
+                    const int32_t* pixels, int64_t npix, const orc_outputs* out, int nthreads) {
+  view v;
+  make_view(s, disc_tex, NULL, &v);
+  v.obj_tex = obj_tex;
+  const int64_t n = pixels ? npix : (int64_t)v.W * v.H;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    int x = pixels ? pixels[2 * i] : (int)(i % v.W);
+    int y = pixels ? pixels[2 * i + 1] : (int)(i / v.W);
+    uint8_t c[4] = {0, 0, 0, 255};
+    int obj = -1;
+    int cls = flat_pixel(&v, x, y, c, &obj);
+    c[3] = 255;
+    if (out->bgra) memcpy(out->bgra + 4 * i, c, 4);
+    if (out->cls) out->cls[i] = (uint8_t)cls;
+    if (out->aux) out->aux[i] = obj;
   }
   return 0;
 }

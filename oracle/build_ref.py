@@ -42,7 +42,7 @@ HEADERS = [
     "camera.h", "constants.h", "math.h", "matrix.h", "object.h", "utility.h",
     "blackhole_solution.h", "object/material.h", "object/object.h",
     "object/object_manager.h", "object/pattern.h", "object/polygon_object.h",
-    "object/vector_object.h",
+    "object/vector_object.h", "ray_tracer.h",
 ]
 # (line number, text that must appear on it) -- guards against a moved loop.
 MARKERS = [

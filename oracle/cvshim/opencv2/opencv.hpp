@@ -42,6 +42,7 @@ enum ImreadModes { IMREAD_COLOR = 1 };
 template <typename T, int n>
 class Vec {
  public:
+  typedef T value_type;
   T val[n];
 
   Vec() { for (int i = 0; i < n; ++i) val[i] = T(0); }

@@ -61,11 +61,15 @@ def load():
     if _lib is None:
         lib = C.CDLL(build())
         lib.orc_render_ref.restype = C.c_int
-        lib.orc_render_ref.argtypes = [C.c_void_p, C.POINTER(OrcTexture), C.c_void_p, C.c_int64,
-                                       C.POINTER(OrcOutputs), C.c_int]
+        lib.orc_render_ref.argtypes = [C.c_void_p, C.POINTER(OrcTexture), C.POINTER(OrcTexture), C.c_void_p,
+                                       C.c_int64, C.POINTER(OrcOutputs), C.c_int]
+        lib.orc_render_flat.restype = C.c_int
+        lib.orc_render_flat.argtypes = [C.c_void_p, C.POINTER(OrcTexture), C.POINTER(OrcTexture), C.c_void_p,
+                                        C.c_int64, C.POINTER(OrcOutputs), C.c_int]
         lib.orc_render_rk4.restype = C.c_int
         lib.orc_render_rk4.argtypes = [C.c_void_p, C.POINTER(OrcTexture), C.POINTER(OrcTexture),
-                                       C.POINTER(OrcRk4Opts), C.c_void_p, C.c_int64, C.POINTER(OrcOutputs), C.c_int]
+                                       C.POINTER(OrcTexture), C.POINTER(OrcRk4Opts), C.c_void_p, C.c_int64,
+                                       C.POINTER(OrcOutputs), C.c_int]
         lib.orc_max_threads.restype = C.c_int
         _lib = lib
     return _lib
@@ -81,15 +85,29 @@ def _tex(t):
 
 def _scene_c(scene):
     """bh_scene POD of a mirror Scene (texture ids are placeholders: the
-    oracle receives the texels directly)."""
-    from blackhole_8_gb300 import capi
+    oracle receives the texels directly). The object table stays alive in
+    the struct's `_keep`."""
     ids = {}
-    if scene.disc is not None:
-        ids[id(scene.disc.texture)] = 0
-    if scene.background is not None:
-        ids[id(scene.background)] = 1
+    for t in scene.textures():
+        ids.setdefault(id(t), len(ids))
     s = scene.to_c(ids)
     return s
+
+
+def _obj_tex(scene):
+    """One OrcTexture per object (empty where it has none), and the arrays
+    that keep the texels alive."""
+    if not scene.objects:
+        return None, []
+    arr = (OrcTexture * len(scene.objects))()
+    keep = []
+    for i, o in enumerate(scene.objects):
+        t = getattr(o, "texture", None)
+        if t is not None:
+            ot, a = _tex(t)
+            arr[i] = ot
+            keep.append(a)
+    return arr, keep
 
 
 def _pixels(pixels):
@@ -110,7 +128,8 @@ def render_ref(scene, pixels=None, threads: int = 0) -> dict:
     bgra = np.zeros((n, 4), np.uint8)
     cls = np.zeros(n, np.uint8)
     out = OrcOutputs(bgra.ctypes.data, cls.ctypes.data, None, None, None, None, None)
-    lib.orc_render_ref(C.byref(s), C.byref(dt) if dt else None, pp, n, C.byref(out), threads)
+    ot, otk = _obj_tex(scene)
+    lib.orc_render_ref(C.byref(s), C.byref(dt) if dt else None, ot, pp, n, C.byref(out), threads)
     res = {"bgra": bgra, "cls": cls}
     if pixels is None:
         h, w = scene.camera.height(), scene.camera.width()
@@ -136,8 +155,27 @@ def render_rk4(scene, step: float = 0.01, max_steps: int = 4000, r_escape: float
     out = OrcOutputs(*(res[k].ctypes.data for k in ("bgra", "cls", "aux", "margin_tex", "margin_r", "b_over_m",
                                                     "steps")))
     opts = OrcRk4Opts(step, max_steps, r_escape)
-    lib.orc_render_rk4(C.byref(s), C.byref(dt) if dt else None, C.byref(bt) if bt else None, C.byref(opts), pp, n,
-                       C.byref(out), threads)
+    ot, otk = _obj_tex(scene)
+    lib.orc_render_rk4(C.byref(s), C.byref(dt) if dt else None, C.byref(bt) if bt else None, ot, C.byref(opts),
+                       pp, n, C.byref(out), threads)
+    if pixels is None:
+        h, w = scene.camera.height(), scene.camera.width()
+        res = {k: v.reshape((h, w) + v.shape[1:]) for k, v in res.items()}
+    return res
+
+
+def render_flat(scene, pixels=None, threads: int = 0) -> dict:
+    """The flat RayTracer (REF ray generation), FP64; aux = object index."""
+    lib = load()
+    s = _scene_c(scene)
+    dt, dta = _tex(scene.disc.texture if scene.disc is not None else None)
+    ot, otk = _obj_tex(scene)
+    pp, n, keep = _pixels(pixels)
+    if pp is None:
+        n = scene.camera.width() * scene.camera.height()
+    res = {"bgra": np.zeros((n, 4), np.uint8), "cls": np.zeros(n, np.uint8), "aux": np.zeros(n)}
+    out = OrcOutputs(res["bgra"].ctypes.data, res["cls"].ctypes.data, res["aux"].ctypes.data, None, None, None, None)
+    lib.orc_render_flat(C.byref(s), C.byref(dt) if dt else None, ot, pp, n, C.byref(out), threads)
     if pixels is None:
         h, w = scene.camera.height(), scene.camera.width()
         res = {k: v.reshape((h, w) + v.shape[1:]) for k, v in res.items()}

@@ -7,21 +7,32 @@
 // ObjectManager<double> (object_manager.h:30-85). It compiles against the
 // project-written OpenCV stand-in in oracle/cvshim.
 //
+// With `mode flat` it runs the reference's flat-space RayTracer instead
+// (ray_tracer.h:52-96): per pixel RayTracer(camera.focus(),
+// camera.PixelVector(x, y, fv)).Prograde(manager, pixel, 10), the loop of
+// ray_tracer_test.cc:140-155; the hole is not inserted then.
+//
 // The reference draws no class buffer (a horizon hit and a miss are both
-// black), so a second "tag" pass replaces the two scene objects by subclasses
+// black), so a second "tag" pass replaces the scene objects by subclasses
 // that override only the virtual colour (material.h:54) with a class tag:
-// 1 = horizon, 2 = disc, 0 = nothing hit. Collision code is inherited as is.
+// 1 = horizon, 2 = disc, 4 = object (channel 1: its index), 0 = nothing hit.
+// Collision code is inherited as is.
 //
 // Usage: ref_runner SCENE_FILE OUT_FILE [--tag] [--threads N] [--time]
 // Scene file (whitespace-separated tokens):
+//   mode curved|flat          (optional, default curved)
 //   image W H
 //   fov RADIANS
 //   bh X Y Z MASS
-//   disc P1x P1y P1z P2x P2y P2z P3x P3y P3z P4x P4y P4z R_OUTER R_INNER
+//   disc P1x P1y P1z P2x P2y P2z P3x P3y P3z P4x P4y P4z R_OUTER R_INNER (optional)
 //   disc_op OP ARGS...        (optional, any number, applied in order)
-//   texture PATH COLS ROWS    (raw BGR bytes, row-major)
+//   texture PATH COLS ROWS    (raw BGR bytes, row-major; the disc's)
+//   rect P1x..P4z PATH COLS ROWS   (Rectangle<double>, textured; PATH - for none)
+//   plane Px Py Pz SIZE       (InfinitePlane<double> with ChessPattern2D{SIZE})
+//   obj_op OP ARGS...         (pose op on the last object line)
 //   frames N
 //   frame K OP ARGS... (K ops) (N times; camera ops for that frame)
+// Objects are inserted after the disc and the hole, in file order.
 // OP is one of MoveTo x y z | Move dx dy dz | MoveX d | MoveY d | MoveZ d |
 //              RotateX a | RotateY a | RotateZ a | Fov a
 // OUT_FILE receives N frames of W*H*3 bytes (BGR), or the tag per pixel in
@@ -43,7 +54,9 @@
 #include "blackhole/camera.h"
 #include "blackhole/object.h"
 #include "blackhole/object/object_manager.h"
+#include "blackhole/object/pattern.h"
 #include "blackhole/blackhole_solution.h"
+#include "blackhole/ray_tracer.h"
 
 namespace {
 
@@ -62,9 +75,30 @@ struct TagAnnulus : blackhole::Annulus<double> {
   cv::Vec3b color(double, double, double) const override { return {2, 0, 0}; }
 };
 
+struct TagRectangle : blackhole::Rectangle<double> {
+  using blackhole::Rectangle<double>::Rectangle;
+  int idx = 0;
+  cv::Vec3b color(double, double, double) const override { return {4, (unsigned char)idx, 0}; }
+};
+
+struct TagPlane : blackhole::InfinitePlane<double> {
+  using blackhole::InfinitePlane<double>::InfinitePlane;
+  int idx = 0;
+  cv::Vec3b color(double, double, double) const override { return {4, (unsigned char)idx, 0}; }
+};
+
 struct Op {
   std::string name;
   double a[3] = {0, 0, 0};
+};
+
+struct ObjSpec {
+  std::string kind;
+  double v[12] = {0};
+  double size = 0;
+  std::string tex_path;
+  int tex_cols = 0, tex_rows = 0;
+  std::vector<Op> ops;
 };
 
 int nargs(const std::string& op) {
@@ -100,6 +134,28 @@ Op read_op(std::istream& in) {
   for (int i = 0; i < n; ++i)
     if (!(in >> op.a[i])) fail("truncated op args");
   return op;
+}
+
+// The flat RayTracer over the frame, as ray_tracer_test.cc:140-155 drives it
+// (pixels are independent; FindCollision is const).
+void render_flat(const blackhole::Camera<value_type>& camera, const blackhole::ObjectManager<value_type>& manager,
+                 cv::Mat* screen, const int kScreenWidth, const int kScreenHeight) {
+  const auto fv = camera.focus_vector();
+#pragma omp parallel for schedule(dynamic, 2)
+  for (int x = 0; x < kScreenWidth; ++x) {
+    for (int y = 0; y < kScreenHeight; ++y) {
+      blackhole::RayTracer ray_tracer(camera.focus(), camera.PixelVector(x, y, fv));
+      ray_tracer.Prograde(manager, screen->data + (y * kScreenWidth + x) * 3, 10);
+    }
+  }
+}
+
+cv::Mat read_texture(const std::string& path, int cols, int rows) {
+  cv::Mat t(rows, cols, CV_8UC3);
+  std::ifstream tf(path, std::ios::binary);
+  tf.read(reinterpret_cast<char*>(t.data), std::streamsize(t.total() * 3));
+  if (!tf) fail("cannot read texture " + path);
+  return t;
 }
 
 // One frame of the reference's render loop. The names the loop uses --
@@ -142,14 +198,38 @@ int main(int argc, char** argv) {
   std::string tex_path;
   int tex_cols = 0, tex_rows = 0;
   std::vector<std::vector<Op>> frames;
+  std::vector<ObjSpec> objs;
+  bool flat = false, have_disc = false;
   std::string key;
   while (in >> key) {
-    if (key == "image") in >> W >> H;
+    if (key == "mode") {
+      std::string m;
+      in >> m;
+      if (m == "flat") flat = true;
+      else if (m != "curved") fail("unknown mode " + m);
+    } else if (key == "tri") {
+      // Triangle<T>'s constructors initialize Object<T>, which is not its
+      // direct base (vector_object.h:26-36): it does not compile instantiated.
+      fail("Triangle<double> does not compile in the reference");
+    } else if (key == "rect" || key == "plane") {
+      ObjSpec o;
+      o.kind = key;
+      const int nv = key == "rect" ? 12 : 3;
+      for (int i = 0; i < nv; ++i) in >> o.v[i];
+      if (key == "rect") in >> o.tex_path >> o.tex_cols >> o.tex_rows;
+      if (key == "plane") in >> o.size;
+      if (!in) fail("truncated " + key);
+      objs.push_back(o);
+    } else if (key == "obj_op") {
+      if (objs.empty()) fail("obj_op before any object");
+      objs.back().ops.push_back(read_op(in));
+    } else if (key == "image") in >> W >> H;
     else if (key == "fov") in >> fov;
     else if (key == "bh") in >> bx >> by >> bz >> mass;
     else if (key == "disc") {
       for (double& v : dp) in >> v;
       in >> r_outer >> r_inner;
+      have_disc = true;
     } else if (key == "disc_op") disc_ops.push_back(read_op(in));
     else if (key == "texture") in >> tex_path >> tex_cols >> tex_rows;
     else if (key == "frames") in >> nframes;
@@ -161,31 +241,63 @@ int main(int argc, char** argv) {
       frames.push_back(ops);
     } else fail("unknown key " + key);
   }
-  if (W <= 0 || H <= 0 || int(frames.size()) != nframes || tex_cols <= 0 || tex_rows <= 0)
+  if (W <= 0 || H <= 0 || int(frames.size()) != nframes || (have_disc && (tex_cols <= 0 || tex_rows <= 0)))
     fail("incomplete scene");
 
-  cv::Mat texture(tex_rows, tex_cols, CV_8UC3);
-  {
-    std::ifstream tf(tex_path, std::ios::binary);
-    tf.read(reinterpret_cast<char*>(texture.data), std::streamsize(texture.total() * 3));
-    if (!tf) fail("cannot read texture");
-  }
-
-  // Insertion order follows the reference's main(): disc first, then the hole.
+  // Insertion order follows the reference's main(): disc first, then the
+  // hole (not in flat mode), then the objects.
   auto& manager = blackhole::ObjectManager<value_type>::GetInstance();
   const point_type p1{dp[0], dp[1], dp[2]}, p2{dp[3], dp[4], dp[5]};
   const point_type p3{dp[6], dp[7], dp[8]}, p4{dp[9], dp[10], dp[11]};
+  if (have_disc) {
+    const cv::Mat texture = read_texture(tex_path, tex_cols, tex_rows);
+    if (tag) {
+      auto d = manager.InsertObject(std::make_unique<TagAnnulus>(p1, p2, p3, p4, r_outer, r_inner));
+      d.second->SetTexture(texture);
+      for (const Op& op : disc_ops) apply(*d.second, op);
+    } else {
+      auto d = manager.InsertObject<blackhole::Annulus>(p1, p2, p3, p4, r_outer, r_inner);
+      d.second->SetTexture(texture);
+      for (const Op& op : disc_ops) apply(*d.second, op);
+    }
+  }
+  std::unique_ptr<blackhole::StaticBlackhole<value_type>> own_hole;
   const blackhole::StaticBlackhole<value_type>* hole = nullptr;
-  if (tag) {
-    auto d = manager.InsertObject(std::make_unique<TagAnnulus>(p1, p2, p3, p4, r_outer, r_inner));
-    d.second->SetTexture(texture);
-    for (const Op& op : disc_ops) apply(*d.second, op);
+  if (flat) {
+    own_hole = std::make_unique<blackhole::StaticBlackhole<value_type>>(point_type(bx, by, bz), mass);
+    hole = own_hole.get();
+  } else if (tag) {
     hole = manager.InsertObject(std::make_unique<TagBlackhole>(point_type(bx, by, bz), mass)).second;
   } else {
-    auto d = manager.InsertObject<blackhole::Annulus>(p1, p2, p3, p4, r_outer, r_inner);
-    d.second->SetTexture(texture);
-    for (const Op& op : disc_ops) apply(*d.second, op);
     hole = manager.InsertObject<blackhole::StaticBlackhole>(point_type(bx, by, bz), mass).second;
+  }
+  for (size_t k = 0; k < objs.size(); ++k) {
+    const ObjSpec& o = objs[k];
+    const double* v = o.v;
+    blackhole::DrawableObject<value_type>* obj = nullptr;
+    if (o.kind == "rect") {
+      const point_type a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]}, d{v[9], v[10], v[11]};
+      if (tag) {
+        auto r = manager.InsertObject(std::make_unique<TagRectangle>(a, b, c, d));
+        r.second->idx = int(k);
+        obj = r.second;
+      } else {
+        auto r = manager.InsertObject<blackhole::Rectangle>(a, b, c, d);
+        if (o.tex_path != "-") r.second->SetTexture(read_texture(o.tex_path, o.tex_cols, o.tex_rows));
+        obj = r.second;
+      }
+    } else {
+      const point_type pos{v[0], v[1], v[2]};
+      if (tag) {
+        auto r = manager.InsertObject(std::make_unique<TagPlane>(pos));
+        r.second->idx = int(k);
+        obj = r.second;
+      } else {
+        obj = manager.InsertObject<blackhole::InfinitePlane>(pos, blackhole::ChessPattern2D<value_type>{int(o.size)})
+                  .second;
+      }
+    }
+    for (const Op& op : o.ops) apply(*obj, op);
   }
 
   std::ofstream out(argv[2], std::ios::binary);
@@ -199,7 +311,8 @@ int main(int argc, char** argv) {
     }
     cv::Mat screen(H, W, CV_8UC3, cv::Scalar(0, 0, 0));
     const auto t0 = std::chrono::steady_clock::now();
-    render_frame(camera, *hole, manager, &screen, W, H);
+    if (flat) render_flat(camera, manager, &screen, W, H);
+    else render_frame(camera, *hole, manager, &screen, W, H);
     const auto t1 = std::chrono::steady_clock::now();
     seconds += std::chrono::duration<double>(t1 - t0).count();
     out.write(reinterpret_cast<const char*>(screen.data), std::streamsize(screen.total() * 3));

@@ -33,20 +33,44 @@ def _op_line(op) -> str:
     return " ".join([op[0]] + [repr(float(a)) for a in op[1:]])
 
 
-def write_scene(path: str, scenes, tex_path: str) -> None:
+def _floats(ps) -> str:
+    return " ".join(repr(float(x)) for p in ps for x in p)
+
+
+def write_scene(path: str, scenes, tex_path: str, flat: bool = False) -> None:
+    from blackhole_8_gb300 import scene as S
     s0 = scenes[0]
     d = s0.disc
-    if d is None:
-        raise ValueError("the reference render needs the disc")
-    tex = d.texture.bgra()[..., :3]
-    tex.tofile(tex_path)
-    lines = [f"image {s0.camera.width()} {s0.camera.height()}",
+    lines = [f"mode {'flat' if flat else 'curved'}",
+             f"image {s0.camera.width()} {s0.camera.height()}",
              f"fov {s0.camera.fov()!r}",
-             "bh " + " ".join(repr(float(x)) for x in s0.hole.position()) + f" {s0.hole.mass()!r}",
-             "disc " + " ".join(repr(float(x)) for p in d.construction for x in p) + f" {d.r_outer()!r} {d.r_inner()!r}"]
-    for op in d.ops:
-        lines.append("disc_op " + _op_line(op))
-    lines.append(f"texture {tex_path} {tex.shape[1]} {tex.shape[0]}")
+             "bh " + " ".join(repr(float(x)) for x in s0.hole.position()) + f" {s0.hole.mass()!r}"]
+    if d is not None:
+        tex = d.texture.bgra()[..., :3]
+        tex.tofile(tex_path)
+        lines.append("disc " + _floats(d.construction) + f" {d.r_outer()!r} {d.r_inner()!r}")
+        for op in d.ops:
+            lines.append("disc_op " + _op_line(op))
+        lines.append(f"texture {tex_path} {tex.shape[1]} {tex.shape[0]}")
+    for k, o in enumerate(s0.objects):
+        if isinstance(o, S.Rectangle):
+            if o.texture is not None:
+                t = o.texture.bgra()[..., :3]
+                tp = f"{tex_path}.obj{k}"
+                t.tofile(tp)
+                tex_spec = f"{tp} {t.shape[1]} {t.shape[0]}"
+            else:
+                tex_spec = "- 0 0"
+            lines.append("rect " + _floats(o.construction) + " " + tex_spec)
+        elif isinstance(o, S.InfinitePlane):
+            size = o.pattern.pattern_size if o.pattern is not None else 0
+            if size != int(size):
+                raise ValueError("the reference's ChessPattern2D takes an integer size")
+            lines.append("plane " + _floats(o.construction) + f" {int(size)}")
+        else:
+            raise ValueError(f"the reference cannot build {type(o).__name__}")
+        for op in o.ops:
+            lines.append("obj_op " + _op_line(op))
     lines.append(f"frames {len(scenes)}")
     for s in scenes:
         if (s.camera.width(), s.camera.height()) != (s0.camera.width(), s0.camera.height()):
@@ -59,13 +83,15 @@ def write_scene(path: str, scenes, tex_path: str) -> None:
         fh.write("\n".join(lines) + "\n")
 
 
-def render(scenes, tag: bool = False, threads: int = 0, timed: bool = False):
-    """Runs the reference loop; returns (frames uint8 [F,H,W,3] BGR, timing)."""
+def render(scenes, tag: bool = False, threads: int = 0, timed: bool = False, flat: bool = False):
+    """Runs the reference loop (flat: its RayTracer); returns (frames uint8
+    [F,H,W,3] BGR, timing). Objects and the disc are taken from the first
+    scene; frames differ by their camera."""
     if not isinstance(scenes, (list, tuple)):
         scenes = [scenes]
     with tempfile.TemporaryDirectory() as td:
         sp, tp, op = (os.path.join(td, n) for n in ("scene.txt", "tex.bin", "out.bin"))
-        write_scene(sp, scenes, tp)
+        write_scene(sp, scenes, tp, flat=flat)
         cmd = [runner(), sp, op]
         if tag:
             cmd.append("--tag")
@@ -82,8 +108,13 @@ def render(scenes, tag: bool = False, threads: int = 0, timed: bool = False):
     return frames, timing
 
 
-def render_with_classes(scene, threads: int = 0):
-    """(BGR image, class per pixel) of one scene from two runner passes."""
-    img, _ = render([scene], threads=threads)
-    tag, _ = render([scene], tag=True, threads=threads)
-    return img[0], tag[0][..., 0].copy()
+def render_with_classes(scene, threads: int = 0, flat: bool = False, with_objects: bool = False):
+    """(BGR image, class per pixel) of one scene from two runner passes;
+    with_objects adds the object index per pixel (-1 elsewhere)."""
+    img, _ = render([scene], threads=threads, flat=flat)
+    tag, _ = render([scene], tag=True, threads=threads, flat=flat)
+    cls = tag[0][..., 0].copy()
+    if not with_objects:
+        return img[0], cls
+    idx = np.where(cls == 4, tag[0][..., 1].astype(np.int32), -1)
+    return img[0], cls, idx

@@ -1,10 +1,12 @@
 """Generates the golden fixtures of the reference's own render.
 
 Runs the reference's render loop (blackhole_solution_test.cc:161-308, built
-into oracle/_ref by oracle/build_ref.py against the OpenCV stand-in) on the
-scenes of tests/helpers.py and stores, per case, the BGR frame and the hit
-class of every pixel (class from the runner's tag pass). Needs the reference
-checkout; the fixtures then pin the oracle and the GPU on hosts without it.
+into oracle/_ref by oracle/build_ref.py against the OpenCV stand-in), or its
+flat RayTracer (ray_tracer.h:52-96) for the flat cases, on the scenes of
+tests/helpers.py and stores, per case, the BGR frame, the hit class of every
+pixel and the index of the object hit (-1: none), the last two from the
+runner's tag pass. Needs the reference checkout; the fixtures then pin the
+oracle and the GPU on hosts without it.
 
 Usage: python tests/golden/make_golden.py
 """
@@ -29,15 +31,17 @@ def main() -> None:
     index = []
     for name, w, h in helpers.GOLDEN_CASES:
         sc = helpers.build(name, w, h)
-        img, cls = refbridge.render_with_classes(sc)
+        flat = name in helpers.FLAT_BUILDERS
+        img, cls, obj = refbridge.render_with_classes(sc, flat=flat, with_objects=True)
         fn = f"ref_{name}_{w}x{h}.npz"
-        np.savez_compressed(os.path.join(HERE, fn), bgr=img, cls=cls)
-        index.append({"file": fn, "builder": name, "width": w, "height": h,
-                      "classes": np.bincount(cls.ravel(), minlength=3).tolist()})
+        np.savez_compressed(os.path.join(HERE, fn), bgr=img, cls=cls, obj=obj)
+        index.append({"file": fn, "builder": name, "width": w, "height": h, "mode": "flat" if flat else "curved",
+                      "classes": np.bincount(cls.ravel(), minlength=5).tolist()})
         print(fn, index[-1]["classes"])
     with open(os.path.join(HERE, "index.json"), "w") as fh:
         json.dump({"generator": "tests/golden/make_golden.py",
-                   "source": "reference render loop blackhole_solution_test.cc:161-308 via oracle/_ref/ref_runner",
+                   "source": "reference render loop blackhole_solution_test.cc:161-308 (flat: RayTracer, "
+                             "ray_tracer.h:52-96) via oracle/_ref/ref_runner",
                    "cases": index}, fh, indent=1)
 
 

@@ -51,14 +51,39 @@ def posed(width: int, height: int) -> S.Scene:
     return sc
 
 
-BUILDERS = {"cfg0_planar": cfg0_planar, "ref_demo": ref_demo, "posed": posed}
+def flat_demo(width: int, height: int) -> S.Scene:
+    """The reference's flat RayTracer scene (ray_tracer_test.cc:50-98)."""
+    return S.flat_demo_scene(width, height)
+
+
+def objects(width: int, height: int) -> S.Scene:
+    """The planar-disc single scene with a chess plane and two panels."""
+    return S.objects_scene(width, height)
+
+
+def triangles(width: int, height: int) -> S.Scene:
+    """The objects scene with two triangles added (checked against the
+    restatement only: the reference's Triangle<T> does not compile when
+    instantiated)."""
+    sc = S.objects_scene(width, height)
+    sc.objects += [S.Triangle((10, -6, -3), (10, 6, -3), (10, 0, 9)), S.Triangle((-4, 9, 5), (6, 9, 5), (0, 9, -3))]
+    return sc
+
+
+BUILDERS = {"cfg0_planar": cfg0_planar, "ref_demo": ref_demo, "posed": posed, "flat_demo": flat_demo,
+            "objects": objects, "triangles": triangles}
 
 GOLDEN_CASES = [
     ("cfg0_planar", 64, 36),
     ("cfg0_planar", 160, 90),
     ("ref_demo", 320, 180),
     ("posed", 80, 45),
+    ("flat_demo", 160, 90),
+    ("objects", 160, 90),
 ]
+
+# builders rendered by the reference's flat RayTracer instead of the curved loop
+FLAT_BUILDERS = {"flat_demo"}
 
 
 def build(name: str, width: int, height: int) -> S.Scene:

@@ -35,7 +35,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.bh_abi_version() == 1
+    assert lib.bh_abi_version() == capi.ABI_VERSION == 2
     o = capi.default_options()
     assert o.integrator == capi.INTEGRATOR_RK4 and o.step == 0.01 and o.max_steps == 4000
     assert o.r_escape == 100.0 and o.block_x * o.block_y % 32 == 0

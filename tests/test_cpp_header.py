@@ -4,6 +4,7 @@ against the in-tree library. On the CPU: the scene built with the C++ classes
 the same bh_scene as the Python mirror (whose poses are pinned by the
 reference's object tests), and the error paths. On the GPU: blackhole::Render
 gives the same frame as the Python renderer and the oracle's hit classes."""
+import ctypes as C
 import os
 import subprocess
 
@@ -40,6 +41,8 @@ def _fields(struct, prefix=""):
         v = getattr(struct, name)
         if hasattr(v, "_fields_"):
             out += _fields(v, prefix + name + ".")
+        elif isinstance(v, C._Pointer):
+            out.append((prefix + name, bool(v)))  # pointers compare by being set
         elif hasattr(v, "__len__"):
             out += [(f"{prefix}{name}[{i}]", x) for i, x in enumerate(v)]
         else:

@@ -51,10 +51,17 @@ def dilate(mask, n=1):
 # the reference's trapezoid scheme
 @pytest.mark.parametrize("case", CASES, ids=lambda c: c["file"])
 def test_trapezoid_fp64_matches_reference(renderer, case):
+    """The reference's curved loop (or, for flat cases, its RayTracer) in
+    FP64 on the GPU against the reference's own output."""
     sc = helpers.build(case["builder"], case["width"], case["height"])
     g = np.load(os.path.join(GOLDEN, case["file"]))
-    o = opts(integrator=capi.INTEGRATOR_REF_TRAPEZOID, precision=capi.PRECISION_FP64, format=capi.FORMAT_BGR8)
-    out = renderer.render([sc], o, hit_class=True)[0]
+    flat = case.get("mode") == "flat"
+    integ = capi.INTEGRATOR_FLAT if flat else capi.INTEGRATOR_REF_TRAPEZOID
+    o = opts(integrator=integ, precision=capi.PRECISION_FP64, format=capi.FORMAT_BGR8)
+    out = renderer.render([sc], o, hit_class=True, aux=flat)[0]
+    if flat:
+        idx = np.where(out.hit_class == capi.CLASS_OBJECT, out.aux, -1).astype(np.int32)
+        assert (idx != g["obj"]).mean() <= 1e-3
     bad = out.hit_class != g["cls"]
     assert bad.mean() <= 1e-3 and not (bad & ~dilate(helpers.class_boundary_mask(g["cls"]))).any()
     diff = (out.pixels != g["bgr"]).any(-1)

@@ -26,9 +26,15 @@ CASES = json.load(open(os.path.join(GOLDEN, "index.json")))["cases"]
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: c["file"])
 def test_oracle_a_matches_reference_fixture(case):
+    """Mode A (the reference's curved loop) or the flat RayTracer against the
+    reference's own output: classes, object indices, colours."""
     sc = helpers.build(case["builder"], case["width"], case["height"])
     g = np.load(os.path.join(GOLDEN, case["file"]))
-    o = oracle.render_ref(sc)
+    if case.get("mode") == "flat":
+        o = oracle.render_flat(sc)
+        assert np.array_equal(np.where(o["cls"] == capi.CLASS_OBJECT, o["aux"], -1).astype(np.int32), g["obj"])
+    else:
+        o = oracle.render_ref(sc)
     assert np.array_equal(o["cls"], g["cls"]), "hit classes differ from the reference"
     diff = (o["bgra"][..., :3] != g["bgr"]).any(-1)
     # colour differences only where a texel-edge tie rounds the other way
@@ -49,7 +55,24 @@ def test_oracle_a_matches_live_reference():
 
 def test_fixture_classes_are_nontrivial():
     for c in CASES:
-        assert min(c["classes"]) > 0, c
+        cl = c["classes"]
+        if c.get("mode") == "flat":
+            assert cl[capi.CLASS_OBJECT] > 0, c
+        else:
+            assert min(cl[:3]) > 0, c
+        if c["builder"] in ("flat_demo", "objects"):
+            g = np.load(os.path.join(GOLDEN, c["file"]))
+            assert len(np.unique(g["obj"][g["obj"] >= 0])) >= 2, c  # several objects seen
+
+
+def test_oracle_objects_tie_order_and_rejections():
+    """On a chord through two coincident planes the later object wins the
+    exact tie (the reference's map visits objects from last to first)."""
+    sc = S.flat_demo_scene(32, 18)
+    sc.objects = [S.InfinitePlane((0.0, 0.0, 0.0), S.ChessPattern2D(10)), S.InfinitePlane((0.0, 0.0, 0.0))]
+    o = oracle.render_flat(sc)
+    hit = o["cls"] == capi.CLASS_OBJECT
+    assert hit.any() and (o["aux"][hit] == 1).all()
 
 
 # ---------------------------------------------------------------------------
