@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-objects", action="store_true", help="skip the objects / flat tracer leg")
     return ap.parse_args()
 
 
@@ -172,6 +173,95 @@ def run_reference(args):
 ADJ_SIDE = 512
 ADJ_WORKLOAD = "adjoint 512x512: MSE vs target at M+5%, disc tilt +3 deg, r_out +2M, yaw/pitch +1 deg; " \
                "gradient w.r.t. M, camera position and yaw/pitch/roll, disc tilt, r_in, r_out; checkpoints every 64 steps"
+
+
+def objects_leg(r, args, cpu: bool):
+    """Times the ordinary-object renders on the GPU (captured sequences,
+    CUDA events, mean of K replays after W) and the reference's own code on
+    the host cores: the flat RayTracer scene of ray_tracer_test.cc panned
+    over 30 frames at 800x450, and the single scene with a chess plane and
+    two panels from 8 azimuths at 1920x1080 (RK4 and the reference's
+    trapezoid scheme)."""
+    import math
+
+    import torch
+
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+    from oracle import refbridge
+
+    def flat_frames(n, w, h):
+        out = []
+        for k in range(n):
+            sc = S.flat_demo_scene(w, h)
+            sc.camera.RotateZ(0.004 * k)
+            out.append(sc)
+        return out
+
+    def object_frames(n, w, h):
+        out = []
+        for k in range(n):
+            sc = S.objects_scene(w, h)
+            sc.camera = S.aimed_camera(w, h, math.radians(60), 20.0, math.radians(80), azimuth=0.05 * k)
+            out.append(sc)
+        return out
+
+    def time_seq(scenes, opts):
+        cs = r.c_scenes(scenes)
+        bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
+                for s in scenes]
+        frames = (capi.Frame * len(scenes))()
+        for i, b in enumerate(bufs):
+            frames[i].pixels = b.data_ptr()
+        seq = r.sequence(cs, frames, opts)
+        stream = torch.cuda.ExternalStream(r.stream)
+        for _ in range(args.warmup):
+            seq.launch()
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            seq.launch()
+        b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        seq.close()
+        rays = sum(s.camera.width() * s.camera.height() for s in scenes)
+        return {"mrays_per_s": round(rays / (ms * 1e-3) / 1e6, 3), "ms_per_step": round(ms, 3)}
+
+    def cpu_ref(scenes, flat):
+        if not cpu:
+            return None
+        try:
+            if not refbridge.available():
+                raise RuntimeError("reference runner unavailable")
+            _, t = refbridge.render(scenes, threads=os.cpu_count() or 1, timed=True, flat=flat)
+            return {"mrays_per_s": round(t["mrays_per_s"], 4), "cores": t["threads"], "kind": "reference",
+                    "sample": f"{len(scenes)} frames"}
+        except Exception as exc:
+            return {"unavailable": str(exc)}
+
+    flat = flat_frames(30, 800, 450)
+    objs = object_frames(8, 1920, 1080)
+    out = {
+        "flat": {
+            "workload": "flat RayTracer scene (ray_tracer_test.cc: 3 textured Rectangles, chess InfinitePlane), "
+                        "30 frames 800x450, 10 chords per ray",
+            "fp32": time_seq(flat, capi.default_options(integrator=capi.INTEGRATOR_FLAT)),
+            "fp64": time_seq(flat, capi.default_options(integrator=capi.INTEGRATOR_FLAT,
+                                                        precision=capi.PRECISION_FP64)),
+            "cpu_reference": cpu_ref(flat[:4], True),
+        },
+        "curved_objects": {
+            "workload": "single scene + chess plane + 2 textured panels, 8 frames 1920x1080",
+            "rk4_fp32_step0.01": time_seq(objs, capi.default_options()),
+            "trapezoid_fp64": time_seq(objs, capi.default_options(integrator=capi.INTEGRATOR_REF_TRAPEZOID,
+                                                                  precision=capi.PRECISION_FP64)),
+            "trapezoid_fp32": time_seq(objs, capi.default_options(integrator=capi.INTEGRATOR_REF_TRAPEZOID)),
+            "cpu_reference_trapezoid": cpu_ref(objs[:2], False),
+        },
+    }
+    return out
 
 
 def adjoint_leg(r, args):
@@ -377,6 +467,10 @@ def run_ours(args):
     if not args.no_adjoint:
         adjoint = adjoint_leg(r, args)
 
+    objects = None
+    if not args.no_objects:
+        objects = objects_leg(r, args, cpu=rank == 0 and not args.no_cpu)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, used, kind, desc = cpu_reference(scenes, CPU_SAMPLE_FRAMES, os.cpu_count() or 1)
@@ -406,7 +500,7 @@ def run_ours(args):
                          "instructions_per_step": capi.RK4_INSTRUCTIONS_PER_STEP, "sm_count": sm_count,
                          "fp64_peak_tflops_measured": round(fp64_tflops, 3)},
             "clocks": clock_info, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
-            "adjoint": adjoint}))
+            "adjoint": adjoint, "objects": objects}))
     r.close()
     if world > 1:
         import torch.distributed as dist

@@ -320,6 +320,76 @@ class Annulus : public Object<T> {
   int32_t mapping_ = BH_DISC_MAP_REF_PLANAR;
 };
 
+// ChessPattern2D<T> (pattern.h:14-50): black and white cells of
+// pattern_size (the reference takes an int).
+template <typename T>
+class ChessPattern2D {
+ public:
+  ChessPattern2D() = default;
+  explicit ChessPattern2D(int pattern_size) : pattern_size_(T(pattern_size)) {}
+  T pattern_size() const { return pattern_size_; }
+
+ private:
+  T pattern_size_ = 1;
+};
+
+// Rectangle<T> (vector_object.h:80-183): corners p1..p4 after the default
+// (0,0,0) vertex; drawn by Rectangle::color from its texture (black without).
+template <typename T>
+class Rectangle : public Object<T> {
+ public:
+  using typename Object<T>::value_type;
+  using typename Object<T>::point_type;
+  Rectangle() : Object<T>({point_type(1, 0, 1), point_type(-1, 0, 1), point_type(-1, 0, -1), point_type(1, 0, -1)}) {}
+  Rectangle(const point_type& p1, const point_type& p2, const point_type& p3, const point_type& p4)
+      : Object<T>({p1, p2, p3, p4}) {}
+  Rectangle(value_type v11, value_type v12, value_type v13, value_type v21, value_type v22, value_type v23,
+            value_type v31, value_type v32, value_type v33, value_type v41, value_type v42, value_type v43)
+      : Rectangle(point_type(v11, v12, v13), point_type(v21, v22, v23), point_type(v31, v32, v33),
+                  point_type(v41, v42, v43)) {}
+  void SetTexture(Texture texture) {
+    if (texture.empty()) throw Error(BH_ERR_EMPTY_TEXTURE, "empty texture");
+    texture_ = std::move(texture);
+  }
+#ifdef BH_GB300_WITH_OPENCV
+  void SetTexture(const cv::Mat& m) { SetTexture(Texture::FromMat(m)); }
+#endif
+  const Texture& texture() const { return texture_; }
+
+ private:
+  Texture texture_;
+};
+
+// Triangle<T> (vector_object.h:18-77): vertices after the default (0,0,0)
+// vertex; drawn black (it has no colour of its own). The reference's own
+// constructors do not compile when instantiated; these take the same
+// arguments.
+template <typename T>
+class Triangle : public Object<T> {
+ public:
+  using typename Object<T>::value_type;
+  using typename Object<T>::point_type;
+  Triangle() : Object<T>({point_type(1, 0, 0), point_type(-1, 0, 0), point_type(0, 0, 1.73)}) {}
+  Triangle(const point_type& a, const point_type& b, const point_type& c) : Object<T>({a, b, c}) {}
+  Triangle(value_type v11, value_type v12, value_type v13, value_type v21, value_type v22, value_type v23,
+           value_type v31, value_type v32, value_type v33)
+      : Triangle(point_type(v11, v12, v13), point_type(v21, v22, v23), point_type(v31, v32, v33)) {}
+};
+
+// InfinitePlane<T> (vector_object.h:187-238): the plane through position()
+// normal to vector_z(), coloured by a ChessPattern2D (black without one).
+template <typename T>
+class InfinitePlane : public Object<T> {
+ public:
+  using typename Object<T>::point_type;
+  explicit InfinitePlane(const point_type& p) : Object<T>(p) {}
+  InfinitePlane(const point_type& p, const ChessPattern2D<T>& pattern) : Object<T>(p), pattern_size_(pattern.pattern_size()) {}
+  T pattern_size() const { return pattern_size_; }
+
+ private:
+  T pattern_size_ = 0;
+};
+
 // Equirectangular sky for escaped rays (not in the reference).
 class Background {
  public:
@@ -356,13 +426,26 @@ struct Options : bh_render_options {
   }
 };
 
-// One scene of a batch.
+// One ordinary object of a scene (exactly one pointer set).
+template <typename T>
+struct SceneObject {
+  const Rectangle<T>* rectangle = nullptr;
+  const Triangle<T>* triangle = nullptr;
+  const InfinitePlane<T>* plane = nullptr;
+  SceneObject(const Rectangle<T>* r) : rectangle(r) {}
+  SceneObject(const Triangle<T>* t) : triangle(t) {}
+  SceneObject(const InfinitePlane<T>* p) : plane(p) {}
+};
+
+// One scene of a batch. The objects' order decides exact distance ties (the
+// later one wins, as in the reference's ObjectManager).
 template <typename T>
 struct Scene {
   const Camera<T>* camera = nullptr;
-  const StaticBlackhole<T>* hole = nullptr;
+  const StaticBlackhole<T>* hole = nullptr;  // may be null with the FLAT integrator
   const Annulus<T>* disc = nullptr;          // may be null
   const Background* background = nullptr;    // may be null
+  std::vector<SceneObject<T>> objects;
 };
 
 template <typename T>
@@ -404,6 +487,34 @@ inline bh_scene ToPod(const Camera<T>& cam, const StaticBlackhole<T>& bh, const 
   return s;
 }
 
+// The bh_object of an object, given the texture id of a rectangle's texture.
+template <typename T>
+inline bh_object ToPod(const SceneObject<T>& so, int32_t tex) {
+  bh_object o;
+  std::memset(&o, 0, sizeof(o));
+  o.texture = -1;
+  if (so.rectangle) {
+    o.type = BH_OBJECT_RECTANGLE;
+    o.texture = tex;
+    const auto& v = so.rectangle->vertex();
+    for (int k = 0; k < 4; ++k) copy3(o.v[k], v[k + 1]);
+  } else if (so.triangle) {
+    o.type = BH_OBJECT_TRIANGLE;
+    const auto& v = so.triangle->vertex();
+    for (int k = 0; k < 3; ++k) copy3(o.v[k], v[k + 1]);
+  } else if (so.plane) {
+    o.type = BH_OBJECT_PLANE;
+    copy3(o.v[0], so.plane->position());
+    copy3(o.axis_x, so.plane->vector_x());
+    copy3(o.axis_y, so.plane->vector_y());
+    copy3(o.axis_z, so.plane->vector_z());
+    o.pattern_size = double(so.plane->pattern_size());
+  } else {
+    throw Error(BH_ERR_INVALID_ARGUMENT, "scene object without an object");
+  }
+  return o;
+}
+
 // Loss and gradient of the differentiable render (bh_render_adjoint).
 struct AdjointResult {
   double loss = 0;
@@ -433,7 +544,7 @@ class Renderer {
   template <typename T>
   void Render(const Camera<T>& cam, const StaticBlackhole<T>& bh, const Annulus<T>* disc, const Background* bg,
               Image& out, const Options& opts = Options()) {
-    std::vector<Scene<T>> one{Scene<T>{&cam, &bh, disc, bg}};
+    std::vector<Scene<T>> one{Scene<T>{&cam, &bh, disc, bg, {}}};
     std::vector<Image> imgs(1);
     Render(one, imgs, opts);
     out = std::move(imgs[0]);
@@ -443,7 +554,8 @@ class Renderer {
   // opts.schedule is BH_SCHEDULE_PERSISTENT).
   template <typename T>
   void Render(const std::vector<Scene<T>>& scenes, std::vector<Image>& out, const Options& opts = Options()) {
-    std::vector<bh_scene> pods = Pods(scenes);
+    std::vector<std::vector<bh_object>> objects;
+    std::vector<bh_scene> pods = Pods(scenes, &objects);
     out.resize(scenes.size());
     std::vector<bh_frame> frames(scenes.size());
     for (size_t i = 0; i < scenes.size(); ++i) {
@@ -466,7 +578,8 @@ class Renderer {
   template <typename T>
   AdjointResult Adjoint(const Scene<T>& scene, const double* theta, const float* d_target, float* d_image = nullptr,
                         float* d_pixel_grad = nullptr, const bh_adjoint_options* opts = nullptr) {
-    std::vector<bh_scene> pods = Pods(std::vector<Scene<T>>{scene});
+    std::vector<std::vector<bh_object>> objects;
+    std::vector<bh_scene> pods = Pods(std::vector<Scene<T>>{scene}, &objects);
     bh_adjoint_frame fr{d_target, d_image, d_pixel_grad};
     bh_adjoint_result r;
     Check(bh_render_adjoint(ctx_, pods.data(), 1, theta, &fr, opts, &r), "bh_render_adjoint");
@@ -499,19 +612,32 @@ class Renderer {
     return id;
   }
 
+  // The scenes' PODs; `objects` holds their object tables during the call.
   template <typename T>
-  std::vector<bh_scene> Pods(const std::vector<Scene<T>>& scenes) {
+  std::vector<bh_scene> Pods(const std::vector<Scene<T>>& scenes, std::vector<std::vector<bh_object>>* objects) {
     std::vector<bh_scene> pods;
     pods.reserve(scenes.size());
-    for (const Scene<T>& s : scenes) {
-      if (!s.camera || !s.hole) throw Error(BH_ERR_INVALID_ARGUMENT, "scene needs a camera and a black hole");
+    objects->assign(scenes.size(), {});
+    const StaticBlackhole<T> no_hole(typename Object<T>::point_type(0, 0, 0), T(1));  // FLAT ignores the hole
+    for (size_t i = 0; i < scenes.size(); ++i) {
+      const Scene<T>& s = scenes[i];
+      if (!s.camera) throw Error(BH_ERR_INVALID_ARGUMENT, "scene needs a camera");
       int32_t dt = -1, bt = -1;
       if (s.disc) {
         if (s.disc->texture().empty()) throw Error(BH_ERR_EMPTY_TEXTURE, "disc has no texture");
         dt = TextureId(s.disc->texture());
       }
       if (s.background) bt = TextureId(s.background->texture());
-      pods.push_back(ToPod(*s.camera, *s.hole, s.disc, dt, bt));
+      bh_scene pod = ToPod(*s.camera, s.hole ? *s.hole : no_hole, s.disc, dt, bt);
+      auto& tab = (*objects)[i];
+      for (const SceneObject<T>& so : s.objects) {
+        int32_t tex = -1;
+        if (so.rectangle && !so.rectangle->texture().empty()) tex = TextureId(so.rectangle->texture());
+        tab.push_back(ToPod(so, tex));
+      }
+      pod.n_objects = int32_t(tab.size());
+      pod.objects = tab.empty() ? nullptr : tab.data();
+      pods.push_back(pod);
     }
     return pods;
   }

@@ -1,6 +1,9 @@
 // Checks of include/blackhole_gb300.hpp, driven by tests/test_cpp_header.py.
 //   hpp_check pod                 the single-scene geometry built with the C++
 //                                 classes, printed as the hex of its bh_scene
+//   hpp_check objects             the objects of the objects scene (a chess
+//                                 plane, two panels, one rotated; a triangle)
+//                                 as bh_objects, one hex line each
 //   hpp_check errors              error paths that need no GPU
 //   hpp_check render W H DISC BG OUT
 //                                 renders the scene (disc RGBA8 1024x64 and sky
@@ -60,6 +63,23 @@ int main(int argc, char** argv) {
     const auto* p = reinterpret_cast<const unsigned char*>(&s);
     for (size_t i = 0; i < sizeof(s); ++i) std::printf("%02x", p[i]);
     std::printf("\n");
+    return 0;
+  }
+  if (mode == "objects") {
+    InfinitePlane<double> plane({0, 0, -6}, ChessPattern2D<double>(2));
+    Rectangle<double> back({12, 8, 8}, {12, -8, 8}, {12, -8, -4}, {12, 8, -4});
+    Rectangle<double> side(-8, -10, 6, 8, -10, 6, 8, -10, -2, -8, -10, -2);
+    side.RotateZ(0.3);
+    side.MoveX(1.5);
+    Triangle<double> tri({10, -6, -3}, {10, 6, -3}, {10, 0, 9});
+    const SceneObject<double> objs[] = {&plane, &back, &side, &tri};
+    const int32_t tex[] = {-1, 3, 4, -1};
+    for (int k = 0; k < 4; ++k) {
+      const bh_object o = ToPod(objs[k], tex[k]);
+      const auto* p = reinterpret_cast<const unsigned char*>(&o);
+      for (size_t i = 0; i < sizeof(o); ++i) std::printf("%02x", p[i]);
+      std::printf("\n");
+    }
     return 0;
   }
   if (mode == "errors") {

@@ -44,7 +44,11 @@ def _fields(struct, prefix=""):
         elif isinstance(v, C._Pointer):
             out.append((prefix + name, bool(v)))  # pointers compare by being set
         elif hasattr(v, "__len__"):
-            out += [(f"{prefix}{name}[{i}]", x) for i, x in enumerate(v)]
+            for i, x in enumerate(v):
+                if hasattr(x, "__len__"):
+                    out += [(f"{prefix}{name}[{i}][{j}]", y) for j, y in enumerate(x)]
+                else:
+                    out.append((f"{prefix}{name}[{i}]", x))
         else:
             out.append((prefix + name, v))
     return out
@@ -61,6 +65,28 @@ def test_cpp_scene_matches_python_mirror(exe):
             assert abs(g - w) <= 1e-13 * max(1.0, abs(w)), (name, g, w)
         else:
             assert g == w, (name, g, w)
+
+
+def test_cpp_objects_match_python_mirror(exe):
+    """Rectangle, Triangle and InfinitePlane of the C++ layer (with pose
+    operations) give the bh_objects of the Python mirror."""
+    out = subprocess.run([exe, "objects"], capture_output=True, text=True, check=True).stdout.split()
+    got = [capi.Object.from_buffer_copy(bytes.fromhex(line)) for line in out]
+    plane = S.InfinitePlane((0, 0, -6), S.ChessPattern2D(2))
+    back = S.Rectangle((12, 8, 8), (12, -8, 8), (12, -8, -4), (12, 8, -4))
+    side = S.Rectangle((-8, -10, 6), (8, -10, 6), (8, -10, -2), (-8, -10, -2))
+    side.RotateZ(0.3)
+    side.MoveX(1.5)
+    tri = S.Triangle((10, -6, -3), (10, 6, -3), (10, 0, 9))
+    back.texture, side.texture = object(), object()
+    ids = {id(back.texture): 3, id(side.texture): 4}
+    want = [o.to_c(ids) for o in (plane, back, side, tri)]
+    for g, w in zip(got, want):
+        for (name, a), (_, b) in zip(_fields(g), _fields(w)):
+            if isinstance(b, float):
+                assert abs(a - b) <= 1e-13 * max(1.0, abs(b)), (name, a, b)
+            else:
+                assert a == b, (name, a, b)
 
 
 def test_cpp_error_paths(exe):
