@@ -88,6 +88,8 @@ struct AdjScene {
       de2_f[kParams][3];
   DevTexture disc_tex, bg_tex;
   int32_t width, height, tiles_x, disc_on, has_bg, scene;
+  int32_t tex32;        // MIXED: FP64 colours take the texture filter in FP32 (tex_sample_at)
+  int32_t pad_;
   int64_t block_begin;  // first block of this scene in the grid
   int64_t ray_begin;    // first ray of this scene (row-major pixels, scenes back to back)
   const float* target;
@@ -420,14 +422,15 @@ BHA_HD void bspline_weights(R f, R w[4], R dw[4]) {
   dw[3] = f2 * R(0.5);
 }
 
-// Colour and its derivatives in s (columns) and u (rows).
+// Colour and its derivatives in s (columns) and u (rows) at cell (cs, cu)
+// with fractions (fs, fu) in [0, 1).
 template <typename R>
-BHA_HD void tex_sample(const DevTexture& t, R s, R u, bool wrap_s, bool wrap_u, R col[3], R dcs[3], R dcu[3]) {
-  const R fs0 = floor(s), fu0 = floor(u);
+BHA_HD void tex_sample_cell(const DevTexture& t, int cs, int cu, R fs, R fu, bool wrap_s, bool wrap_u, R col[3],
+                            R dcs[3], R dcu[3]) {
   R ws[4], dws[4], wu[4], dwu[4];
-  bspline_weights(s - fs0, ws, dws);
-  bspline_weights(u - fu0, wu, dwu);
-  const int bs = int(fs0) - 1, bu = int(fu0) - 1;
+  bspline_weights(fs, ws, dws);
+  bspline_weights(fu, wu, dwu);
+  const int bs = cs - 1, bu = cu - 1;
   int is[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) is[k] = tex_index(bs + k, t.width, wrap_s);
@@ -455,6 +458,36 @@ BHA_HD void tex_sample(const DevTexture& t, R s, R u, bool wrap_s, bool wrap_u, 
       dcu[ch] = fma(dwu[j], row[ch], dcu[ch]);
     }
   }
+}
+
+// Colour and its derivatives in s (columns) and u (rows).
+template <typename R>
+BHA_HD void tex_sample(const DevTexture& t, R s, R u, bool wrap_s, bool wrap_u, R col[3], R dcs[3], R dcu[3]) {
+  const R fs0 = floor(s), fu0 = floor(u);
+  tex_sample_cell(t, int(fs0), int(fu0), s - fs0, u - fu0, wrap_s, wrap_u, col, dcs, dcu);
+}
+
+// The texture filter of a colour in precision R. With s.tex32 (MIXED) an
+// FP64 colour takes the sample point in FP64 -- the cell and the fraction
+// exactly, the fraction then rounded to FP32 (~6e-8 texel) -- and the
+// B-spline weights and texel sums in FP32 (~1e-7 of the colour): an FP64
+// filter costs ~250 FP64 operations per sample, the largest FP64 load of the
+// band rays' crossings. The FP64 mode keeps it in FP64.
+template <typename S, typename R>
+BHA_HD void tex_sample_at(const S& s, const DevTexture& t, R a, R b, bool wrap_s, bool wrap_u, R col[3], R dcs[3],
+                          R dcu[3]) {
+  if (sizeof(R) == sizeof(double) && s.tex32) {
+    const R fa = floor(a), fb = floor(b);
+    float c[3], da[3], db[3];
+    tex_sample_cell<float>(t, int(fa), int(fb), float(a - fa), float(b - fb), wrap_s, wrap_u, c, da, db);
+    for (int ch = 0; ch < 3; ++ch) {
+      col[ch] = R(c[ch]);
+      dcs[ch] = R(da[ch]);
+      dcu[ch] = R(db[ch]);
+    }
+    return;
+  }
+  tex_sample(t, a, b, wrap_s, wrap_u, col, dcs, dcu);
 }
 
 template <typename R>
@@ -593,7 +626,7 @@ BHA_HD void crossing_colour(const AdjScene& s, const RayC<R, P>& rc, P dm, Cross
   const R az = atan2(c.Y1, c.X1);
   c.tc_s = (c.Rr - rc.r_in) / (rc.r_out - rc.r_in) * R(s.disc_tex.width) - R(0.5);
   c.tc_u = az * R(s.disc_tex.height / kTwoPiD) - R(0.5);
-  tex_sample(s.disc_tex, c.tc_s, c.tc_u, false, true, col, dcs, dcu);
+  tex_sample_at(s, s.disc_tex, c.tc_s, c.tc_u, false, true, col, dcs, dcu);
 }
 
 // Field access by precision.
@@ -669,7 +702,7 @@ BHA_HD void escape_eval(const AdjScene& s, const AdjParams& p, const RayC<R, P>&
   const int W = s.bg_tex.width, H = s.bg_tex.height;
   e.ts = (e.lon + R(kPiD)) * R(W / kTwoPiD) - R(0.5);
   e.tu = (R(kPiD / 2) - e.lat) * R(H / kPiD) - R(0.5);
-  tex_sample(s.bg_tex, e.ts, e.tu, true, false, col, dcs, dcu);
+  tex_sample_at(s, s.bg_tex, e.ts, e.tu, true, false, col, dcs, dcu);
 }
 
 // ---------------------------------------------------------------------------

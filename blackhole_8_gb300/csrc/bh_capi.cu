@@ -1389,6 +1389,7 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
     AdjScene* a = ctx->h_adj.ptr + i;
     std::memset(a, 0, sizeof(*a));
     build_adj_scene(scenes[i], th, o.softness, a);
+    a->tex32 = o.precision == BH_PRECISION_MIXED ? 1 : 0;
     a->disc_on = posed.disc.enabled ? 1 : 0;
     if (a->disc_on) {
       const TexEntry& t = ctx->textures[posed.disc.texture];

@@ -125,11 +125,11 @@ def test_precisions_and_band(renderer):
     rmw, _, _ = _run(renderer, [sc], None, [target], capi.adjoint_options(band=1e3))
     assert np.isfinite(g32[0]).all() and np.isfinite(np.array(r32[0].grad)).all()
     assert rm0[0].band_rays == 0 and r64[0].band_rays == 0
-    # every ray in the band: FP64 forward (the FP64 call's colours) and an FP32
-    # reverse pass
+    # every ray in the band: FP64-accurate forward with the texture filter in
+    # FP32 (colours within ~1e-7 of the FP64 call's) and an FP32 reverse pass
     assert rmw[0].band_rays == 64 * 64
     g, g64 = np.array(rmw[0].grad), np.array(r64[0].grad)
-    assert np.linalg.norm(g - g64) <= 1e-5 * np.linalg.norm(g64)
+    assert np.linalg.norm(g - g64) <= 5e-5 * np.linalg.norm(g64)
     assert abs(rmw[0].loss - r64[0].loss) <= 1e-6 * r64[0].loss
 
 
