@@ -385,6 +385,7 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->half_h_f = float(d->half_h);
   d->inv_mass_f = float(1.0 / d->mass);
   d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
+  bhgb::resolve_rk4_constants(d->Fhat, d->Fhat_f, &d->Flen, &d->Flen_f, &d->x0, &d->x0_f, d->F, d->mass);
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;

@@ -62,11 +62,13 @@ struct DevScene {
   double r_in, r_out;
   double s1_len, s2_len;
   double half_w, half_h;      // W / 2.0, H / 2.0
+  double Fhat[3], Flen, x0;   // RK4: F / |F|, |F|, M / |F| - 1/3 (the same for every ray)
 
   float F_f[3], E0_f[3], vy_f[3], vz_f[3];
   float dc_f[3], dn_f[3], dv1_f[3], ds1_f[3], ds2_f[3], de1_f[3], de2_f[3];
   float mass_f, b_c_f, r_h_f, r_in_f, r_out_f, s1_len_f, s2_len_f, half_w_f, half_h_f;
   float inv_mass_f;
+  float Fhat_f[3], Flen_f, x0_f;
   float b_lip;                // bound on |b(x+1) - b(x)| / M along an image row (row_b_lipschitz)
 
   DevTexture disc_tex;
@@ -197,6 +199,24 @@ inline float setup_band_for(double band, double setup_band) {
 // Resolves a bh_object for the device, relative to the hole at h (host).
 // Edges are formed in world coordinates as the reference forms them;
 // the rectangle's normal is cv::normalize(e1 x e2) = v * (1 / |v|).
+// The RK4 ray's per-scene constants: every ray of a scene starts at F (the
+// camera relative to the hole), so the unit vector F / |F|, which is also the
+// first axis of each ray's orbital basis rotated to the camera, and the
+// initial x = M / |F| - 1/3 are the scene's.
+inline void resolve_rk4_constants(double* Fhat, float* Fhat_f, double* Flen, float* Flen_f, double* x0, float* x0_f,
+                                  const double F[3], double mass) {
+  const double L = std::sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+  const double k = L > 0 ? 1.0 / L : 0.0;
+  for (int i = 0; i < 3; ++i) {
+    Fhat[i] = F[i] * k;
+    Fhat_f[i] = float(Fhat[i]);
+  }
+  *Flen = L;
+  *Flen_f = float(L);
+  *x0 = L > 0 ? mass / L - 1.0 / 3.0 : 0.0;
+  *x0_f = float(*x0);
+}
+
 inline void resolve_object(const bh_object& b, const double h[3], DevTexture tex, DevObject* d) {
   std::memset(d, 0, sizeof(*d));
   d->type = b.type;

@@ -214,6 +214,35 @@ __device__ __forceinline__ PlaneRay<R> make_ray(const DevScene& s, int x, int y)
   return r;
 }
 
+// The RK4 ray of pixel (x, y): F1 = F . e^ and b = |F x e^| (e^ the unit ray
+// direction), and X0, the second axis of the ray's orbital basis rotated to
+// the camera (the first is the scene's F / |F|): F = F1 e^ + b x^ with x^ the
+// in-plane normal of e^, so X0 = (x^ F1 - e^ b) / |F| = (F^ F1 - e^ |F|) / b
+// = F x (F x e^) / (|F| b). Both come from the cross product, which keeps
+// them accurate to rounding where |F| - F1 would cancel (near-critical rays
+// seen from afar).
+template <typename R>
+struct RkRay {
+  V3<R> X0;
+  R F1, b;
+};
+
+template <typename R>
+__device__ __forceinline__ RkRay<R> make_ray_rk4(const DevScene& s, int x, int y) {
+  const R a = BH_S(R, s, half_w) - R(x);
+  const R c = BH_S(R, s, half_h) - R(y);
+  const V3<R> yv = normalize(BH_V(R, s, E0) + BH_V(R, s, vy) * a + BH_V(R, s, vz) * c);
+  const R L = BH_S(R, s, Flen);
+  const V3<R> F = BH_V(R, s, F);
+  const V3<R> fx = cross(F, yv);
+  RkRay<R> r;
+  r.F1 = dot(yv, F);
+  r.b = length(fx);
+  const R ilb = r.b > R(0) ? R(1) / (L * r.b) : R(0);
+  r.X0 = cross(F, fx) * ilb;
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // REF_TRAPEZOID: blackhole_solution_test.cc:185-296 with
 // StaticBlackhole::G / InvSqrtG / SolveG (blackhole_solution.h:27-53),
@@ -574,7 +603,8 @@ struct RayState {
   R ev;         // event payload: u at the disc crossing
   int k, kc;    // steps taken, step index holding the next crossing
   int status;
-  V3<R> yv, xv;  // in-plane basis rotated to the camera: position = r (cos(phi - phi0) yv + sin(phi - phi0) xv)
+  V3<R> xv;     // with the scene's F / |F|, the ray's orbital basis rotated to the
+                // camera: position = r (cos(phi - phi0) F^ + sin(phi - phi0) xv)
 };
 
 // Sets up the RK4 state from a plane ray computed in precision RS.
@@ -585,28 +615,20 @@ __device__ __forceinline__ float inv_mass<float>(const DevScene& s) { return s.i
 template <>
 __device__ __forceinline__ double inv_mass<double>(const DevScene& s) { return 1.0 / s.mass; }
 
-// Sets up the RK4 state of a plane ray; everything in precision R.
+// Sets up the RK4 state of a ray; everything in precision R. The camera sits
+// at angle phi0 = atan2(b, F1) from the ray direction; the basis rotated by
+// phi0 (F^, X0) measures every later angle from the camera, so phi0 itself is
+// only needed for the aux output.
 template <typename R>
-__device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& ray, R h, RayState<R>& st) {
+__device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray, R h, RayState<R>& st) {
   const R M = BH_S(R, s, mass);
   st.k = 0;
   st.kc = 0x7fffffff;
   st.dcr = R(0);
   st.ev = R(0);
   const R bm = ray.b * inv_mass<R>(s);
-  const R rr = ray.F1 * ray.F1 + ray.b * ray.b;
-  const R x0 = M * rnorm(ray.F0 * ray.F0 + rr) - R(1.0 / 3.0);
-  // The camera sits at angle phi0 = atan2(b, F1) in the (yv, xv) plane. The
-  // basis rotated by phi0 measures every later angle from the camera, so no
-  // arctangent is needed for phi0 itself (only for the aux output).
-  R c0 = R(1), s0 = R(0);
-  if (rr > R(0)) {
-    const R ir = rnorm(rr);
-    c0 = ray.F1 * ir;
-    s0 = ray.b * ir;
-  }
-  st.yv = ray.yv * c0 + ray.xv * s0;
-  st.xv = ray.xv * c0 - ray.yv * s0;
+  const R x0 = BH_S(R, s, x0);
+  st.xv = ray.X0;
   st.phi0 = s.aux ? atan2(ray.b, ray.F1) : R(0);
   st.x = x0;
   if (!(bm > R(1e-6))) {  // heads into the centre
@@ -622,7 +644,7 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const PlaneRay<R>& r
   st.status = kRunning;
   if (s.disc_on) {
     const V3<R> n = BH_V(R, s, dn);
-    const R A = dot(n, st.yv), B = dot(n, st.xv);
+    const R A = dot(n, BH_V(R, s, Fhat)), B = dot(n, st.xv);
     if (A * A + B * B > R(1e-24)) {
       // the line of nodes: crossings at d + j pi, d in (0, pi]
       R d = atan2(B, A) + kPi<R>() * R(0.5);
@@ -780,7 +802,7 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     const R rw = shade_div(BH_S(R, s, mass), st.ev);
     R sp, cp;
     shade_sincos(phic, &sp, &cp);
-    const V3<R> p = st.yv * (rw * cp) + st.xv * (rw * sp);
+    const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
     hit.cls = BH_CLASS_DISC;
     hit.aux = float(R(1) / st.ev);
     hit.bgra = disc_color(s, p);
@@ -812,7 +834,7 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
       shade_sincos(phie, &sp, &cp);
       const R k = rnorm(we * we + c.u_esc * c.u_esc);
       const R cd = -we * k, sd = c.u_esc * k;
-      const V3<R> d = st.yv * (cp * cd - sp * sd) + st.xv * (sp * cd + cp * sd);
+      const V3<R> d = BH_V(R, s, Fhat) * (cp * cd - sp * sd) + st.xv * (sp * cd + cp * sd);
       hit.bgra = background_color(s, d);
     }
   }
@@ -827,7 +849,7 @@ constexpr double kBC = 5.196152422706632;  // 3 sqrt(3)
 template <typename R, bool kMixed>
 __device__ Hit trace_rk4(const DevScene& s, int x, int y, const Rk4Consts<R>& c, int* steps) {
   RayState<R> st;
-  init_rk4<R>(s, make_ray<R>(s, x, y), c.h, st);
+  init_rk4<R>(s, make_ray_rk4<R>(s, x, y), c.h, st);
   *steps = advance_rk4<R, kMixed>(s, st, c, 0x7fffffff);
   return finish_rk4<R>(s, st, c);
 }
@@ -841,7 +863,7 @@ __device__ Hit trace_rk4(const DevScene& s, int x, int y, const Rk4Consts<R>& c,
 template <typename R>
 __device__ Hit trace_rk4_obj(const DevScene& s, int x, int y, const Rk4Consts<R>& c, int* steps) {
   RayState<R> st;
-  init_rk4<R>(s, make_ray<R>(s, x, y), c.h, st);
+  init_rk4<R>(s, make_ray_rk4<R>(s, x, y), c.h, st);
   const R M = BH_S(R, s, mass);
   V3<R> prev = BH_V(R, s, F);
   int k = 0;
@@ -865,7 +887,7 @@ __device__ Hit trace_rk4_obj(const DevScene& s, int x, int y, const Rk4Consts<R>
       const R rn = M / un;
       R sp, cp;
       sincos(R(k + 1) * c.h, &sp, &cp);
-      const V3<R> next = st.yv * (rn * cp) + st.xv * (rn * sp);
+      const V3<R> next = BH_V(R, s, Fhat) * (rn * cp) + st.xv * (rn * sp);
       V3<R> hp;
       R bd = R(0);
       const int best = nearest_object<R>(s, prev, next, &bd, &hp);
@@ -918,7 +940,7 @@ __device__ __noinline__ double eps_fp64(const DevScene& s, int x, int y) {
 // The FP64 band test of the mixed tracer: an FP32 prefilter on b, then the
 // FP64 first integral of the candidates. setup_mixed and the classification
 // pass make the same decision (same code, same ray).
-__device__ __forceinline__ bool band_candidate(const DevScene& s, const PlaneRay<float>& r, const LaunchParams& p) {
+__device__ __forceinline__ bool band_candidate(const DevScene& s, const RkRay<float>& r, const LaunchParams& p) {
   return fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band;
 }
 __device__ __forceinline__ bool in_band_eps(double eps, const LaunchParams& p) {
@@ -931,7 +953,7 @@ __device__ __forceinline__ bool in_band_eps(double eps, const LaunchParams& p) {
 // integral from FP64; everything else of the setup is FP32.
 __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, const LaunchParams& p,
                                             RayState<float>& st) {
-  const PlaneRay<float> r = make_ray<float>(s, x, y);
+  const RkRay<float> r = make_ray_rk4<float>(s, x, y);
   init_rk4<float>(s, r, p.c32.h, st);
   if (band_candidate(s, r, p)) {
     const double eps = eps_fp64(s, x, y);
@@ -1064,7 +1086,7 @@ __device__ __forceinline__ bool take_fp32_ray(const LaunchParams& p, int scene, 
   const DevScene& s = p.scenes[scene];
   if (!ray_pixel(s, item - s.ray_begin, px, py)) return false;
   if (!kMixed) {
-    init_rk4<float>(s, make_ray<float>(s, *px, *py), p.c32.h, st);
+    init_rk4<float>(s, make_ray_rk4<float>(s, *px, *py), p.c32.h, st);
     return true;
   }
   // a band ray is traced by the FP64 pass (listed by classify_band_kernel)
@@ -1121,7 +1143,7 @@ __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
         const int y = (int)(hseg / segs_x);
         const int x = ((int)(hseg - (long long)y * segs_x) << 5) + lane;
         if (x >= s.width) continue;
-        const PlaneRay<float> r = make_ray<float>(s, x, y);
+        const RkRay<float> r = make_ray_rk4<float>(s, x, y);
         if (!(fabsf(r.b * s.inv_mass_f - float(kBC)) < p.class_band)) continue;
         const double eps = eps_fp64(s, x, y);
         if (!in_band_eps(eps, p)) continue;
@@ -1231,7 +1253,7 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
             const DevScene& s = p.scenes[scene];
             if (ray_pixel(s, ray - s.ray_begin, &px, &py)) {
               ++rays;
-              init_rk4<R>(s, make_ray<R>(s, px, py), h, st);
+              init_rk4<R>(s, make_ray_rk4<R>(s, px, py), h, st);
             }
           } else {
             scene = pend_scene;
