@@ -284,6 +284,26 @@ def test_sequence_graph_matches_direct_render(renderer):
     seq.close()
 
 
+def test_host_render_in_chunks_matches_device_render(renderer):
+    """bh_render of more than 64 M pixels over >= 8 scenes renders in chunks
+    whose copy-back overlaps the next chunk: frames equal the device render
+    and the statistics cover every chunk."""
+    torch = pytest.importorskip("torch")
+    scenes = S.flythrough(8, 2900, 2900)
+    o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, step=0.1)
+    host = renderer.render(scenes, o)
+    st = renderer.stats()
+    assert st.rays == 8 * 2900 * 2900 and st.flags == 0
+    assert st.d2h_bytes == 8 * 2900 * 2900 * 4
+    bufs, frames = _device_frames(torch, scenes, with_cls=False)
+    renderer.render_device(renderer.c_scenes(scenes), frames, o)
+    torch.cuda.synchronize()
+    sd = renderer.stats()
+    assert (sd.rays, sd.steps, sd.band_rays) == (st.rays, st.steps, st.band_rays)
+    for (px, _), h in zip(bufs, host):
+        assert np.array_equal(px.cpu().numpy(), h.pixels)
+
+
 def test_render_device_on_torch_stream(renderer):
     torch = pytest.importorskip("torch")
     scenes = [S.single_scene(64, 36)]
