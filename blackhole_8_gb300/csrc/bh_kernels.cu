@@ -978,7 +978,10 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
   if ((threadIdx.x & 31) == __ffs(m) - 1 && lo) atomicAdd(dst, (unsigned long long)lo);
 }
 
-// GRID schedule: one thread per pixel, gridDim.z = scene.
+// GRID schedule: one thread per pixel, gridDim.z = scene; one kernel per
+// precision and integrator, each with the registers (and the occupancy) of
+// its own variant.
+template <int kPrecision, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   const DevScene& s = p.scenes[blockIdx.z];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -987,11 +990,11 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   Hit h;
   int steps = 0;
   int band_ray = 0;
-  if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
-    h = p.precision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
-  } else if (p.precision == BH_PRECISION_FP64) {
+  if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+    h = kPrecision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
+  } else if (kPrecision == BH_PRECISION_FP64) {
     h = trace_rk4<double, false>(s, x, y, p.c64, &steps);
-  } else if (p.precision == BH_PRECISION_MIXED) {
+  } else if (kPrecision == BH_PRECISION_MIXED) {
     RayState<float> st;
     if (setup_mixed(s, x, y, p, st)) {
       steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
@@ -1014,9 +1017,19 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   }
 }
 
-// GRID schedule for the FLAT integrator and for scenes with objects (FP32 or
-// FP64): a kernel of its own, so that the object code does not raise the
-// register count of grid_kernel.
+template <typename R>
+__device__ __forceinline__ const Rk4Consts<R>& rk4_consts(const LaunchParams& p);
+template <>
+__device__ __forceinline__ const Rk4Consts<float>& rk4_consts<float>(const LaunchParams& p) { return p.c32; }
+template <>
+__device__ __forceinline__ const Rk4Consts<double>& rk4_consts<double>(const LaunchParams& p) { return p.c64; }
+
+// GRID schedule for the FLAT integrator and for scenes with objects: one
+// kernel per precision and integrator, so that the object code does not
+// raise the register count of grid_kernel and each variant gets the
+// occupancy of its own registers (FP32 RK4 with objects: 64, where one
+// kernel over all six variants took 128).
+template <typename R, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   const DevScene& s = p.scenes[blockIdx.z];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1024,15 +1037,14 @@ __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   if (x >= s.width || y >= s.height) return;
   Hit h;
   int steps = 0;
-  const bool fp64 = p.precision == BH_PRECISION_FP64;
-  if (p.integrator == BH_INTEGRATOR_FLAT) {
-    h = fp64 ? trace_flat<double>(s, x, y) : trace_flat<float>(s, x, y);
-  } else if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
-    h = fp64 ? trace_ref<double, true>(s, x, y) : trace_ref<float, true>(s, x, y);
+  if (kIntegrator == BH_INTEGRATOR_FLAT) {
+    h = trace_flat<R>(s, x, y);
+  } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+    h = trace_ref<R, true>(s, x, y);
   } else if (s.n_objects > 0) {
-    h = fp64 ? trace_rk4_obj<double>(s, x, y, p.c64, &steps) : trace_rk4_obj<float>(s, x, y, p.c32, &steps);
+    h = trace_rk4_obj<R>(s, x, y, rk4_consts<R>(p), &steps);
   } else {
-    h = fp64 ? trace_rk4<double, false>(s, x, y, p.c64, &steps) : trace_rk4<float, false>(s, x, y, p.c32, &steps);
+    h = trace_rk4<R, false>(s, x, y, rk4_consts<R>(p), &steps);
   }
   store_hit(s, p.format, x, y, h);
   if (p.counters) {
@@ -1355,8 +1367,33 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
   }
   const dim3 block(block_x, block_y, 1);
   const dim3 grid((max_w + block_x - 1) / block_x, (max_h + block_y - 1) / block_y, p.n_scenes);
-  if (objects) grid_objects_kernel<<<grid, block, 0, stream>>>(p);
-  else grid_kernel<<<grid, block, 0, stream>>>(p);
+  void (*kernel)(LaunchParams);
+  const bool fp64 = p.precision == BH_PRECISION_FP64;
+  if (!objects) {
+    if (p.integrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+      kernel = fp64 ? grid_kernel<BH_PRECISION_FP64, BH_INTEGRATOR_REF_TRAPEZOID>
+                    : grid_kernel<BH_PRECISION_FP32, BH_INTEGRATOR_REF_TRAPEZOID>;
+    } else if (p.precision == BH_PRECISION_MIXED) {
+      kernel = grid_kernel<BH_PRECISION_MIXED, BH_INTEGRATOR_RK4>;
+    } else {
+      kernel = fp64 ? grid_kernel<BH_PRECISION_FP64, BH_INTEGRATOR_RK4> : grid_kernel<BH_PRECISION_FP32, BH_INTEGRATOR_RK4>;
+    }
+    kernel<<<grid, block, 0, stream>>>(p);
+    return cudaGetLastError();
+  }
+  switch (p.integrator) {
+    case BH_INTEGRATOR_FLAT:
+      kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_FLAT> : grid_objects_kernel<float, BH_INTEGRATOR_FLAT>;
+      break;
+    case BH_INTEGRATOR_REF_TRAPEZOID:
+      kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_REF_TRAPEZOID>
+                    : grid_objects_kernel<float, BH_INTEGRATOR_REF_TRAPEZOID>;
+      break;
+    default:
+      kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_RK4> : grid_objects_kernel<float, BH_INTEGRATOR_RK4>;
+      break;
+  }
+  kernel<<<grid, block, 0, stream>>>(p);
   return cudaGetLastError();
 }
 
