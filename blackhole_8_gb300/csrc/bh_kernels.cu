@@ -96,6 +96,48 @@ struct Pick<double> {
 template <typename R>
 __device__ __forceinline__ R kPi() { return R(CUDART_PI); }
 
+// Division, sine/cosine and atan2 of the setup and the shading: fast forms
+// in FP32 (a quotient within 2 ulp; sin/cos within ~1e-6 rad over the angles
+// a ray sweeps; atan2 within ~2e-7 rad), against ~3e-3 rad per sky texel and
+// the FP32 integration's own ~1e-5 rad; the exact ones in FP64.
+template <typename R>
+__device__ __forceinline__ R shade_div(R a, R b) { return a / b; }
+template <>
+__device__ __forceinline__ float shade_div<float>(float a, float b) { return __fdividef(a, b); }
+template <typename R>
+__device__ __forceinline__ void shade_sincos(R x, R* s, R* c) { sincos(x, s, c); }
+template <>
+__device__ __forceinline__ void shade_sincos<float>(float x, float* s, float* c) { __sincosf(x, s, c); }
+
+// atan2 in FP32: reduction to t = min(|x|, |y|) / max(|x|, |y|) in [0, 1],
+// atan(t) = t P(t^2) with P the degree-7 minimax polynomial of atan(t) / t
+// on [0, 1] (Remez exchange on the absolute error of t P(t^2), fitted by
+// csrc/atan_poly_fit.py: |error| <= 3.8e-8 in exact arithmetic), then the
+// octant: pi/2 - r above the diagonal, pi - r for x < 0, the sign of y.
+// atan2(0, 0) = 0.
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  const float t = mx > 0.f ? __fdividef(mn, mx) : 0.f;
+  const float z = t * t;
+  float p = -4.0545672e-3f;
+  p = fmaf(p, z, 2.1862958e-2f);
+  p = fmaf(p, z, -5.5912327e-2f);
+  p = fmaf(p, z, 9.6421973e-2f);
+  p = fmaf(p, z, -1.3908630e-1f);
+  p = fmaf(p, z, 1.9946566e-1f);
+  p = fmaf(p, z, -3.3329861e-1f);
+  p = fmaf(p, z, 9.9999934e-1f);
+  float r = p * t;
+  if (ay > ax) r = 1.57079633f - r;
+  if (x < 0.f) r = 3.14159265f - r;
+  return copysignf(r, y);
+}
+template <typename R>
+__device__ __forceinline__ R shade_atan2(R y, R x) { return atan2(y, x); }
+template <>
+__device__ __forceinline__ float shade_atan2<float>(float y, float x) { return atan2_poly(y, x); }
+
 // ---------------------------------------------------------------------------
 // textures and pixels
 __device__ __forceinline__ uchar4 texel(const DevTexture& t, long long idx) {
@@ -136,9 +178,9 @@ __device__ uchar4 disc_color_polar(const DevScene& s, V3<R> hit) {
   const V3<R> q = hit - BH_V(R, s, dc);
   const R rr = length(q);
   const R rin = BH_S(R, s, r_in), rout = BH_S(R, s, r_out);
-  int tx = (int)floor((rr - rin) / (rout - rin) * R(s.disc_tex.width));
+  int tx = (int)floor(shade_div(rr - rin, rout - rin) * R(s.disc_tex.width));
   tx = min(max(tx, 0), s.disc_tex.width - 1);
-  R a = atan2(dot(BH_V(R, s, de2), q), dot(BH_V(R, s, de1), q)) * (R(0.5) / kPi<R>());
+  R a = shade_atan2(dot(BH_V(R, s, de2), q), dot(BH_V(R, s, de1), q)) * (R(0.5) / kPi<R>());
   a -= floor(a);
   int ty = (int)floor(a * R(s.disc_tex.height));
   ty = min(max(ty, 0), s.disc_tex.height - 1);
@@ -154,11 +196,17 @@ __device__ __forceinline__ uchar4 disc_color(const DevScene& s, V3<R> hit) {
 template <typename R>
 __device__ uchar4 background_color(const DevScene& s, V3<R> d) {
   const int W = s.bg_tex.width, H = s.bg_tex.height;
-  const R lon = atan2(d.y, d.x);
-  const R lat = asin(fmin(fmax(d.z, R(-1)), R(1)));
+  const R lon = shade_atan2(d.y, d.x);
+  // angle from the +z pole: pi/2 - asin(z), in FP32 as atan2(|(x, y)|, z)
+  R colat;
+  if constexpr (sizeof(R) == 4) {
+    colat = atan2_poly(sqrtf(d.x * d.x + d.y * d.y), d.z);
+  } else {
+    colat = kPi<R>() * R(0.5) - asin(fmin(fmax(d.z, R(-1)), R(1)));
+  }
   int tx = (int)floor((lon + kPi<R>()) * (R(W) * R(0.5) / kPi<R>()));
   tx = tx >= W ? tx - W : (tx < 0 ? 0 : tx);
-  int ty = (int)floor((kPi<R>() * R(0.5) - lat) * (R(H) / kPi<R>()));
+  int ty = (int)floor(colat * (R(H) / kPi<R>()));
   ty = min(max(ty, 0), H - 1);
   return texel(s.bg_tex, (long long)ty * W + tx);
 }
@@ -238,7 +286,7 @@ __device__ __forceinline__ RkRay<R> make_ray_rk4(const DevScene& s, int x, int y
   RkRay<R> r;
   r.F1 = dot(yv, F);
   r.b = length(fx);
-  const R ilb = r.b > R(0) ? R(1) / (L * r.b) : R(0);
+  const R ilb = r.b > R(0) ? shade_div(R(1), L * r.b) : R(0);
   r.X0 = cross(F, fx) * ilb;
   return r;
 }
@@ -637,7 +685,7 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
     st.eps = R(0);
     return;
   }
-  const R mb = M / ray.b;
+  const R mb = shade_div(M, ray.b);
   const R eps = mb * mb - R(1.0 / 27.0);
   st.eps = eps;
   st.w = copysign(sqrt(fmax(eps + x0 * x0 * fma(R(2), x0, R(1)), R(0))), ray.F1);
@@ -647,11 +695,11 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
     const R A = dot(n, BH_V(R, s, Fhat)), B = dot(n, st.xv);
     if (A * A + B * B > R(1e-24)) {
       // the line of nodes: crossings at d + j pi, d in (0, pi]
-      R d = atan2(B, A) + kPi<R>() * R(0.5);
+      R d = shade_atan2(B, A) + kPi<R>() * R(0.5);
       if (d > kPi<R>()) d -= kPi<R>();
       if (d <= R(0)) d += kPi<R>();
       st.dcr = d;
-      st.kc = (int)floor(d / h);
+      st.kc = (int)floor(shade_div(d, h));
     }
   }
 }
@@ -669,7 +717,7 @@ __device__ __forceinline__ RC crossing_u(const RayState<R>& st, R h) {
 template <typename RC>
 __device__ __forceinline__ bool on_disc(const DevScene& s, RC u) {
   if (!(u < RC(0.5))) return false;
-  const RC rc = BH_S(RC, s, mass) / u;
+  const RC rc = shade_div(BH_S(RC, s, mass), u);
   return rc >= BH_S(RC, s, r_in) && rc <= BH_S(RC, s, r_out);
 }
 
@@ -695,7 +743,7 @@ __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R
   R u = crossing_u<R>(st, h);
   bool hit = on_disc<R>(s, u);
   if (kRefine64) {
-    const R rc = BH_S(R, s, mass) / u;
+    const R rc = shade_div(BH_S(R, s, mass), u);
     const R tol = R(2e-3) * BH_S(R, s, mass);
     if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
       const CrossU r64 = crossing_u_fp64(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
@@ -708,7 +756,7 @@ __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R
     return true;
   }
   st.dcr += kPi<R>();
-  st.kc = (int)floor(st.dcr / h);
+  st.kc = (int)floor(shade_div(st.dcr, h));
   return false;
 }
 
@@ -779,18 +827,6 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
   return taken;
 }
 
-// Division and sine/cosine of the shading: CUDA's fast forms in FP32 (a
-// quotient within 2 ulp; sin/cos within ~1e-6 rad over the angles a ray
-// sweeps, against ~3e-3 rad per sky texel), the exact ones in FP64.
-template <typename R>
-__device__ __forceinline__ R shade_div(R a, R b) { return a / b; }
-template <>
-__device__ __forceinline__ float shade_div<float>(float a, float b) { return __fdividef(a, b); }
-template <typename R>
-__device__ __forceinline__ void shade_sincos(R x, R* s, R* c) { sincos(x, s, c); }
-template <>
-__device__ __forceinline__ void shade_sincos<float>(float x, float* s, float* c) { __sincosf(x, s, c); }
-
 // Shades a finished RK4 ray.
 template <typename R>
 __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c) {
@@ -804,7 +840,7 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     shade_sincos(phic, &sp, &cp);
     const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
     hit.cls = BH_CLASS_DISC;
-    hit.aux = float(R(1) / st.ev);
+    if (s.aux) hit.aux = float(R(1) / st.ev);
     hit.bgra = disc_color(s, p);
   } else if (st.status == kEscape) {
     // Cubic Hermite through (xa, wa) and (x, w) over the last step; Newton
