@@ -22,7 +22,7 @@ BH_ERR_TIMEOUT = -7
 BH_ERR_NO_DEVICE = -8
 BH_ERR_DEVICE_FAULT = -9
 
-INTEGRATOR_REF_TRAPEZOID, INTEGRATOR_RK4, INTEGRATOR_FLAT = 0, 1, 2
+INTEGRATOR_REF_TRAPEZOID, INTEGRATOR_RK4, INTEGRATOR_FLAT, INTEGRATOR_MULTI = 0, 1, 2, 3
 PRECISION_FP32, PRECISION_FP64, PRECISION_MIXED = 0, 1, 2
 RAYGEN_REF, RAYGEN_PINHOLE = 0, 1
 DISC_MAP_REF_PLANAR, DISC_MAP_POLAR = 0, 1
@@ -32,7 +32,8 @@ SCHEDULE_GRID, SCHEDULE_PERSISTENT = 0, 1
 CLASS_MISS, CLASS_HORIZON, CLASS_DISC, CLASS_MAXSTEPS, CLASS_OBJECT = 0, 1, 2, 3, 4
 OBJECT_RECTANGLE, OBJECT_TRIANGLE, OBJECT_PLANE = 1, 2, 3
 MAX_OBJECTS = 64
-ABI_VERSION = 2
+MAX_HOLES = 8
+ABI_VERSION = 3
 RK4_ALGO_FLOPS_PER_STEP = 50  # BH_RK4_ALGO_FLOPS_PER_STEP: the roofline unit
 RK4_FLOPS_PER_STEP = 28
 RK4_INSTRUCTIONS_PER_STEP = 18
@@ -62,7 +63,8 @@ class Object(C.Structure):
 
 class Scene(C.Structure):
     _fields_ = [("camera", Camera), ("hole", Hole), ("disc", Disc), ("background", C.c_int32),
-                ("n_objects", C.c_int32), ("objects", C.POINTER(Object))]
+                ("n_objects", C.c_int32), ("objects", C.POINTER(Object)), ("n_extra_holes", C.c_int32),
+                ("reserved_holes", C.c_int32), ("extra_holes", C.POINTER(Hole))]
 
 
 class Frame(C.Structure):

@@ -188,14 +188,14 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
   if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4 &&
-      o.integrator != BH_INTEGRATOR_FLAT)
+      o.integrator != BH_INTEGRATOR_FLAT && o.integrator != BH_INTEGRATOR_MULTI)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
   if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
   if (o.integrator != BH_INTEGRATOR_RK4 && o.precision == BH_PRECISION_MIXED)
     return set_err(ctx, BH_ERR_UNSUPPORTED, "MIXED precision applies to the RK4 integrator only");
-  if (o.integrator == BH_INTEGRATOR_FLAT && o.schedule != BH_SCHEDULE_GRID)
-    return set_err(ctx, BH_ERR_UNSUPPORTED, "the FLAT integrator runs on the GRID schedule");
+  if ((o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI) && o.schedule != BH_SCHEDULE_GRID)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "the FLAT and MULTI integrators run on the GRID schedule");
   if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE)
     return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown raygen %d", o.raygen);
   if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8)
@@ -274,6 +274,57 @@ int validate_objects(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_opti
   return BH_OK;
 }
 
+// The holes of a MULTI scene relative to the scene's hole: hole 0 is the
+// scene's own. Centre of mass and total mass into cen / mtot.
+int scene_holes(const bh_scene& s, double (*pos)[3], double* mass, double cen[3], double* mtot) {
+  const int n = 1 + (s.n_extra_holes > 0 ? s.n_extra_holes : 0);
+  *mtot = 0;
+  cen[0] = cen[1] = cen[2] = 0;
+  for (int j = 0; j < n; ++j) {
+    const bh_hole& b = j == 0 ? s.hole : s.extra_holes[j - 1];
+    for (int k = 0; k < 3; ++k) pos[j][k] = b.position[k] - s.hole.position[k];
+    mass[j] = b.mass;
+    *mtot += b.mass;
+    for (int k = 0; k < 3; ++k) cen[k] += b.mass * pos[j][k];
+  }
+  for (int k = 0; k < 3; ++k) cen[k] /= *mtot;
+  return n;
+}
+
+int validate_holes(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_options& o) {
+  if (s.n_extra_holes < 0 || s.n_extra_holes > BH_MAX_HOLES - 1)
+    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: n_extra_holes must be in [0, %d]", i, BH_MAX_HOLES - 1);
+  if (s.n_extra_holes > 0) {
+    if (!s.extra_holes) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d: extra_holes is NULL", i);
+    if (o.integrator != BH_INTEGRATOR_MULTI)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: extra holes need the MULTI integrator", i);
+    for (int j = 0; j < s.n_extra_holes; ++j) {
+      const bh_hole& b = s.extra_holes[j];
+      if (!finite3(b.position) || !(b.mass > 0) || !std::isfinite(b.mass))
+        return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "scene %d extra hole %d: mass must be positive and finite", i, j);
+    }
+  }
+  if (o.integrator != BH_INTEGRATOR_MULTI) return BH_OK;
+  double pos[BH_MAX_HOLES][3], mass[BH_MAX_HOLES], cen[3], mtot;
+  const int n = scene_holes(s, pos, mass, cen, &mtot);
+  const double R = o.r_escape * mtot;
+  auto dist = [&](const double* a) {
+    const double d[3] = {a[0] - s.hole.position[0] - cen[0], a[1] - s.hole.position[1] - cen[1],
+                         a[2] - s.hole.position[2] - cen[2]};
+    return std::sqrt(dot3(d, d));
+  };
+  for (int j = 0; j < n; ++j) {
+    const double d[3] = {pos[j][0] - cen[0], pos[j][1] - cen[1], pos[j][2] - cen[2]};
+    if (std::sqrt(dot3(d, d)) + 2 * mass[j] >= R)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: hole %d reaches the escape sphere", i, j);
+  }
+  if (dist(s.camera.position) >= R)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: camera lies outside the escape sphere", i);
+  if (s.disc.enabled && dist(s.disc.center) + s.disc.r_outer >= R)
+    return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: disc extends past the escape sphere", i);
+  return BH_OK;
+}
+
 int validate_scene(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_options& o) {
   const bh_camera& c = s.camera;
   if (c.width < 1 || c.height < 1 || c.width > 32768 || c.height > 32768)
@@ -286,6 +337,7 @@ int validate_scene(bh_ctx* ctx, const bh_scene& s, int i, const bh_render_option
   if (s.background != -1 && !texture_ok(ctx, s.background))
     return set_err(ctx, BH_ERR_BAD_TEXTURE, "scene %d: background texture %d is not valid", i, s.background);
   if (int rc = validate_objects(ctx, s, i, o)) return rc;
+  if (int rc = validate_holes(ctx, s, i, o)) return rc;
   const double rel[3] = {c.position[0] - s.hole.position[0], c.position[1] - s.hole.position[1],
                          c.position[2] - s.hole.position[2]};
   if (o.integrator == BH_INTEGRATOR_RK4 && std::sqrt(dot3(rel, rel)) >= o.r_escape * s.hole.mass)
@@ -393,6 +445,22 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->inv_mass_f = float(1.0 / d->mass);
   d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
   bhgb::resolve_rk4_constants(d->Fhat, d->Fhat_f, &d->Flen, &d->Flen_f, &d->x0, &d->x0_f, d->F, d->mass);
+  {
+    double pos[BH_MAX_HOLES][3], mass[BH_MAX_HOLES], cen[3], mtot;
+    d->n_holes = scene_holes(s, pos, mass, cen, &mtot);
+    for (int j = 0; j < d->n_holes; ++j) {
+      bhgb::DevHole& t = d->holes[j];
+      for (int k = 0; k < 3; ++k) {
+        t.p[k] = pos[j][k];
+        t.p_f[k] = float(pos[j][k]);
+      }
+      t.hm = 0.5 * mass[j];
+      t.hm_f = float(t.hm);
+    }
+    set3(d->mcen, d->mcen_f, cen[0], cen[1], cen[2]);
+    d->r_esc = o.r_escape * mtot;
+    d->r_esc_f = float(d->r_esc);
+  }
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
@@ -508,7 +576,8 @@ int enqueue_kernels(bh_ctx* ctx, LaunchParams& p, const bh_render_options& o, co
       w[i] = scenes[i].camera.width;
       h[i] = scenes[i].camera.height;
     }
-    const bool objects = o.integrator == BH_INTEGRATOR_FLAT || count_objects(scenes, n) > 0;
+    const bool objects = o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI ||
+                         count_objects(scenes, n) > 0;
     BH_CUDA(ctx, bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, st, objects));
   } else {
     int blocks = 0;
@@ -900,7 +969,8 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
         h[i] = scenes[i].camera.height;
       }
       e = bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, cs,
-                            o.integrator == BH_INTEGRATOR_FLAT || q->n_objects_total > 0);
+                            o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI ||
+                                q->n_objects_total > 0);
     } else {
       e = bhgb::launch_persistent(p, o.threads_per_block, blocks, cs);
     }
@@ -1418,6 +1488,8 @@ int bh_render_adjoint(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const doub
     }
     if (scenes[i].n_objects != 0)
       return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: the differentiable render draws no objects", i);
+    if (scenes[i].n_extra_holes != 0)
+      return set_err(ctx, BH_ERR_UNSUPPORTED, "scene %d: the differentiable render traces one hole", i);
     bh_scene posed;
     scene_at_theta(scenes[i], th, &posed);
     if ((rc = validate_scene(ctx, posed, i, ro))) return rc;

@@ -38,6 +38,16 @@ struct DevObject {
   int32_t pad;
 };
 
+// A hole of the MULTI integrator, relative to the scene's hole: position and
+// half its mass (the term m / (2 rho) of the conformal factor), in FP64 and
+// rounded once to FP32 (one 16-byte load).
+struct alignas(16) DevHole {
+  double p[3];
+  double hm;
+  float p_f[3];
+  float hm_f;
+};
+
 // One scene resolved for the device. Positions are relative to the hole.
 // The FP64 block drives the FP64 paths; the FP32 block is the same data
 // rounded once on the host.
@@ -81,7 +91,11 @@ struct DevScene {
   int64_t ray_begin;          // first ray index of this scene (persistent)
   const DevObject* objects;   // this scene's objects (n_objects of them)
   int32_t n_objects;
-  int32_t pad_objects;
+  int32_t n_holes;            // MULTI: holes[0] is the scene's hole, then the extra holes
+  double mcen[3];             // MULTI: the holes' centre of mass (escape sphere centre)
+  double r_esc;               // MULTI: escape sphere radius, r_escape * total mass
+  float mcen_f[3], r_esc_f;
+  DevHole holes[BH_MAX_HOLES];
   uint8_t* pixels;
   uint8_t* cls;
   float* aux;

@@ -955,6 +955,181 @@ __device__ Hit trace_rk4_obj(const DevScene& s, int x, int y, const Rk4Consts<R>
   return finish_rk4<R>(s, st, c);
 }
 
+// ---------------------------------------------------------------------------
+// MULTI: several holes. Null rays of the static metric
+//   ds^2 = -a^2 dt^2 + p^4 |dx|^2,  p = 1 + S,  a = (1 - S) / (1 + S),
+//   S = sum_i m_i / (2 |x - x_i|)
+// in isotropic coordinates (one hole: Schwarzschild). Their spatial paths are
+// the rays of the index n = p^2 / a = (1 + S)^3 / (1 - S) (Fermat): with s
+// the Euclidean arc length and T the unit tangent,
+//   dx/ds = T,  dT/ds = g - T (T . g),  g = grad ln n = (3 / (1 + S) + 1 / (1 - S)) grad S.
+// One evaluation: the bending g - T (T . g) at (x, T), S at x and the
+// squared distance to the nearest hole centre.
+template <typename R>
+struct MultiEval {
+  V3<R> a;
+  R S, d2;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_hole(const DevHole& h, V3<R>* p, R* hm);
+template <>
+__device__ __forceinline__ void load_hole<float>(const DevHole& h, V3<float>* p, float* hm) {
+  const float4 q = *reinterpret_cast<const float4*>(h.p_f);
+  *p = {q.x, q.y, q.z};
+  *hm = q.w;
+}
+template <>
+__device__ __forceinline__ void load_hole<double>(const DevHole& h, V3<double>* p, double* hm) {
+  *p = {h.p[0], h.p[1], h.p[2]};
+  *hm = h.hm;
+}
+
+template <typename R>
+__device__ __forceinline__ MultiEval<R> multi_eval(const DevScene& s, V3<R> x, V3<R> T) {
+  R S = R(0), d2 = R(3e38);
+  V3<R> gS = {R(0), R(0), R(0)};
+  for (int i = 0; i < s.n_holes; ++i) {
+    V3<R> p;
+    R hm;
+    load_hole<R>(s.holes[i], &p, &hm);
+    const V3<R> d = x - p;
+    const R r2 = dot(d, d);
+    const R ir = rnorm(r2);
+    const R k = hm * ir;
+    S += k;
+    gS = gS - d * (k * ir * ir);
+    d2 = fmin(d2, r2);
+  }
+  const R f = shade_div(R(3), R(1) + S) + shade_div(R(1), R(1) - S);
+  const V3<R> g = gS * f;
+  return {g - T * dot(T, g), S, d2};
+}
+
+// Cubic Hermite through (x0, h T0) and (x1, h T1) at t: position and d/dt.
+template <typename R>
+__device__ __forceinline__ void hermite3(V3<R> x0, V3<R> m0, V3<R> x1, V3<R> m1, R t, V3<R>* p, V3<R>* dp) {
+  const R t2 = t * t, t3 = t2 * t;
+  *p = x0 * (R(2) * t3 - R(3) * t2 + R(1)) + m0 * (t3 - R(2) * t2 + t) + x1 * (R(3) * t2 - R(2) * t3) +
+       m1 * (t3 - t2);
+  *dp = x0 * (R(6) * t2 - R(6) * t) + m0 * (R(3) * t2 - R(4) * t + R(1)) + x1 * (R(6) * t - R(6) * t2) +
+        m1 * (R(3) * t2 - R(2) * t);
+}
+
+// One ray of the MULTI integrator, all in precision R, positions relative to
+// the scene's hole. Each step: RK4 in s with h = step * (distance to the
+// nearest hole); the disc is found on the step's Hermite curve (the sign of
+// n . (x - c) changes; three Newton steps for the crossing from the chord's
+// estimate), the objects on the step's chord. Within a step the earlier
+// event wins (the disc on ties), as in the RK4 render with objects; a ray
+// whose S reaches 0.9 is captured; one that leaves the escape sphere moving
+// outward escapes in the direction of the Hermite tangent where the curve
+// meets the sphere (three Newton steps).
+template <typename R>
+__device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>& c, int* steps) {
+  const R a_ = BH_S(R, s, half_w) - R(px);
+  const R c_ = BH_S(R, s, half_h) - R(py);
+  const V3<R> T0 = normalize(BH_V(R, s, E0) + BH_V(R, s, vy) * a_ + BH_V(R, s, vz) * c_) * R(-1);
+  const V3<R> cen = BH_V(R, s, mcen);
+  const R resc = BH_S(R, s, r_esc);
+  V3<R> X = BH_V(R, s, F), T = T0;
+  MultiEval<R> e = multi_eval<R>(s, X, T);
+  Hit hit = {make_uchar4(0, 0, 0, 255), BH_CLASS_MAXSTEPS, 0.f};
+  int k = 0;
+  for (;; ++k) {
+    if (e.S >= R(0.9)) {
+      hit.cls = BH_CLASS_HORIZON;
+      break;
+    }
+    if (k >= c.kmax) break;
+    const R h = c.h * sqrt(e.d2), hh = h * R(0.5);
+    const V3<R> t2 = T + e.a * hh;
+    const MultiEval<R> e2 = multi_eval<R>(s, X + T * hh, t2);
+    const V3<R> t3 = T + e2.a * hh;
+    const MultiEval<R> e3 = multi_eval<R>(s, X + t2 * hh, t3);
+    const V3<R> t4 = T + e3.a * h;
+    const MultiEval<R> e4 = multi_eval<R>(s, X + t3 * h, t4);
+    const R h6 = h * R(1.0 / 6.0);
+    const V3<R> Xn = X + (T + (t2 + t3) * R(2) + t4) * h6;
+    const V3<R> Tn = normalize(T + (e.a + (e2.a + e3.a) * R(2) + e4.a) * h6);
+    // disc crossing on the step's curve
+    R f_disc = R(2);
+    V3<R> dhit;
+    if (s.disc_on) {
+      const V3<R> dn = BH_V(R, s, dn), dc = BH_V(R, s, dc);
+      const R g0 = dot(dn, X - dc), g1 = dot(dn, Xn - dc);
+      if ((g0 > R(0)) != (g1 > R(0))) {
+        R t = g0 != g1 ? shade_div(g0, g0 - g1) : R(0.5);
+        V3<R> p, dp;
+        for (int i = 0; i < 3; ++i) {
+          hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
+          const R dd = dot(dn, dp);
+          if (dd != R(0)) t = fmin(fmax(t - shade_div(dot(dn, p - dc), dd), R(0)), R(1));
+        }
+        hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
+        const R rr = length(p - dc);
+        if (rr >= BH_S(R, s, r_in) && rr <= BH_S(R, s, r_out)) {
+          f_disc = t;
+          dhit = p;
+        }
+      }
+    }
+    // objects on the step's chord
+    R f_obj = R(2);
+    Hit ho;
+    if (s.n_objects > 0) {
+      V3<R> hp;
+      R bd = R(0);
+      const int best = nearest_object<R>(s, X, Xn, &bd, &hp);
+      if (best >= 0) {
+        const V3<R> ch = Xn - X;
+        f_obj = sqrt(shade_div(bd, dot(ch, ch)));
+        ho.cls = BH_CLASS_OBJECT;
+        ho.aux = float(best);
+        ho.bgra = object_color<R>(s.objects[best], hp);
+      }
+    }
+    if (f_disc <= R(1) && f_disc <= f_obj) {
+      hit.cls = BH_CLASS_DISC;
+      hit.aux = float(length(dhit - BH_V(R, s, dc)) / BH_S(R, s, mass));
+      hit.bgra = disc_color(s, dhit);
+      ++k;
+      break;
+    }
+    if (f_obj <= R(1)) {
+      hit = ho;
+      ++k;
+      break;
+    }
+    const V3<R> q = Xn - cen;
+    if (dot(q, q) >= resc * resc && dot(Tn, q) > R(0)) {
+      // the curve meets the escape sphere: |p(t) - cen|^2 = resc^2
+      const V3<R> q0 = X - cen;
+      const R r0 = length(q0), r1 = length(q);
+      R t = r1 != r0 ? fmin(fmax(shade_div(resc - r0, r1 - r0), R(0)), R(1)) : R(1);
+      V3<R> p, dp;
+      for (int i = 0; i < 3; ++i) {
+        hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
+        const V3<R> w = p - cen;
+        const R dd = R(2) * dot(w, dp);
+        if (dd != R(0)) t = fmin(fmax(t - shade_div(dot(w, w) - resc * resc, dd), R(0)), R(1));
+      }
+      hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
+      const V3<R> Te = normalize(dp);
+      hit.cls = BH_CLASS_MISS;
+      hit.aux = float(atan2(length(cross(T0, Te)), dot(T0, Te)));
+      if (s.has_bg) hit.bgra = background_color(s, Te);
+      ++k;
+      break;
+    }
+    X = Xn;
+    T = Tn;
+    e = multi_eval<R>(s, X, T);
+  }
+  *steps = k;
+  return hit;
+}
+
 // FP64 trace of a band ray (out of line: keeps FP64 register pressure away
 // from the FP32 callers).
 __device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
@@ -1060,7 +1235,7 @@ __device__ __forceinline__ const Rk4Consts<float>& rk4_consts<float>(const Launc
 template <>
 __device__ __forceinline__ const Rk4Consts<double>& rk4_consts<double>(const LaunchParams& p) { return p.c64; }
 
-// GRID schedule for the FLAT integrator and for scenes with objects: one
+// GRID schedule for the FLAT and MULTI integrators and for scenes with objects: one
 // kernel per precision and integrator, so that the object code does not
 // raise the register count of grid_kernel and each variant gets the
 // occupancy of its own registers (FP32 RK4 with objects: 64, where one
@@ -1075,6 +1250,8 @@ __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   int steps = 0;
   if (kIntegrator == BH_INTEGRATOR_FLAT) {
     h = trace_flat<R>(s, x, y);
+  } else if (kIntegrator == BH_INTEGRATOR_MULTI) {
+    h = trace_multi<R>(s, x, y, rk4_consts<R>(p), &steps);
   } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
     h = trace_ref<R, true>(s, x, y);
   } else if (s.n_objects > 0) {
@@ -1424,6 +1601,9 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
     case BH_INTEGRATOR_REF_TRAPEZOID:
       kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_REF_TRAPEZOID>
                     : grid_objects_kernel<float, BH_INTEGRATOR_REF_TRAPEZOID>;
+      break;
+    case BH_INTEGRATOR_MULTI:
+      kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_MULTI> : grid_objects_kernel<float, BH_INTEGRATOR_MULTI>;
       break;
     default:
       kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_RK4> : grid_objects_kernel<float, BH_INTEGRATOR_RK4>;

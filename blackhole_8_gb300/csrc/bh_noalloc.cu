@@ -153,8 +153,8 @@ int check(const bh_scene* scenes, int32_t n, const bh_device_texture* tex, int32
           const bh_render_options& o, int64_t* total, char* err, int32_t len) {
   if (!scenes || !frames || n < 1 || n > BH_NOALLOC_MAX_SCENES)
     return fail(err, len, BH_ERR_INVALID_ARGUMENT, "need 1..%d scenes with frames", BH_NOALLOC_MAX_SCENES);
-  if (o.integrator == BH_INTEGRATOR_FLAT)
-    return fail(err, len, BH_ERR_UNSUPPORTED, "the no-alloc render has no FLAT integrator");
+  if (o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI)
+    return fail(err, len, BH_ERR_UNSUPPORTED, "the no-alloc render has no FLAT or MULTI integrator");
   if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4)
     return fail(err, len, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
   if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED ||
@@ -189,6 +189,8 @@ int check(const bh_scene* scenes, int32_t n, const bh_device_texture* tex, int32
       return fail(err, len, BH_ERR_BAD_TEXTURE, "scene %d: background texture %d is not valid", i, s.background);
     if (s.n_objects != 0)
       return fail(err, len, BH_ERR_UNSUPPORTED, "scene %d: the no-alloc render draws no objects", i);
+    if (s.n_extra_holes != 0)
+      return fail(err, len, BH_ERR_UNSUPPORTED, "scene %d: the no-alloc render traces one hole", i);
     if (frames[i].aux && o.integrator != BH_INTEGRATOR_RK4)
       return fail(err, len, BH_ERR_UNSUPPORTED, "frame %d: aux output needs the RK4 integrator", i);
     const double rel[3] = {c.position[0] - s.hole.position[0], c.position[1] - s.hole.position[1],

@@ -371,6 +371,7 @@ class Scene:
     background: Texture | None = None
     meta: dict = field(default_factory=dict)
     objects: list = field(default_factory=list)  # Rectangle / Triangle / InfinitePlane, in table order
+    extra_holes: list = field(default_factory=list)  # further StaticBlackholes (MULTI integrator)
 
     def textures(self) -> list:
         """Every texture the scene draws with."""
@@ -379,8 +380,9 @@ class Scene:
         return out
 
     def to_c(self, texture_ids: dict) -> capi.Scene:
-        """The C scene; its object table lives in the returned struct's
-        `_keep` attribute, which the caller keeps alive while the C ABI reads it."""
+        """The C scene; its object and extra-hole tables live in the returned
+        struct's `_keep` attribute, which the caller keeps alive while the C
+        ABI reads it."""
         s = capi.Scene()
         s.camera = self.camera.to_c()
         s.hole = self.hole.to_c()
@@ -390,12 +392,18 @@ class Scene:
             s.disc.enabled = 0
             s.disc.texture = -1
         s.background = texture_ids[id(self.background)] if self.background is not None else -1
-        s._keep = None
+        keep = []
         if self.objects:
             arr = (capi.Object * len(self.objects))(*[o.to_c(texture_ids) for o in self.objects])
             s.objects = C.cast(arr, C.POINTER(capi.Object))
             s.n_objects = len(self.objects)
-            s._keep = arr
+            keep.append(arr)
+        if self.extra_holes:
+            harr = (capi.Hole * len(self.extra_holes))(*[h.to_c() for h in self.extra_holes])
+            s.extra_holes = C.cast(harr, C.POINTER(capi.Hole))
+            s.n_extra_holes = len(self.extra_holes)
+            keep.append(harr)
+        s._keep = keep or None
         return s
 
 
@@ -533,6 +541,24 @@ def single_scene(width: int = 640, height: int = 360, seed: int = 0) -> Scene:
     cam = aimed_camera(width, height, math.radians(60), 20.0, math.radians(80))
     return Scene(cam, StaticBlackhole((0.0, 0.0, 0.0), 1.0), equatorial_disc(6.0, 20.0, disc_tex), bg,
                  {"workload": f"single {width}x{height}"})
+
+
+def binary_scene(width: int = 640, height: int = 360, seed: int = 0, separation: float = 6.0,
+                 mass_ratio: float = 1.0, inclination_deg: float = 80.0, radius: float = 30.0) -> Scene:
+    """Two holes for the MULTI integrator (isotropic coordinates): total mass
+    1 split m1 : m2 = 1 : mass_ratio, on the y axis `separation` apart about
+    their centre of mass at the origin; a circumbinary disc from
+    1.4 separation to 20 in the z = 0 plane (polar map); the camera at
+    `radius` from the origin, `inclination_deg` from the disc normal, in the
+    x-z plane (an equal-mass scene is mirror symmetric in y)."""
+    disc_tex, bg = standard_textures(seed)
+    m1 = 1.0 / (1.0 + mass_ratio)
+    m2 = 1.0 - m1
+    h1 = StaticBlackhole((0.0, -separation * m2, 0.0), m1)
+    h2 = StaticBlackhole((0.0, separation * m1, 0.0), m2)
+    cam = aimed_camera(width, height, math.radians(60), radius, math.radians(inclination_deg))
+    return Scene(cam, h1, equatorial_disc(1.4 * separation, 20.0, disc_tex), bg,
+                 {"workload": f"binary {width}x{height}"}, extra_holes=[h2])
 
 
 def panel_texture(seed: int, width: int = 160, height: int = 120) -> Texture:

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define BH_ABI_VERSION 2
+#define BH_ABI_VERSION 3
 
 /* ---- status codes -------------------------------------------------------- */
 enum {
@@ -59,8 +59,22 @@ enum {
  * BasicLinearRayRecurrence, driven as in ray_tracer_test.cc:140-155): ten
  * straight chords from the focus through the PixelVector point, the step
  * scaled by 100 / |step|^2 when |step|^2 < 100, tested against the objects
- * and the disc; the hole does not bend or stop it (GRID schedule only). */
-enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1, BH_INTEGRATOR_FLAT = 2 };
+ * and the disc; the hole does not bend or stop it (GRID schedule only).
+ * MULTI traces the scene's hole and its extra_holes together (the reference
+ * only sketches this, multiple_blackhole_solution_test.cc:149-262, by
+ * averaging per-hole plane solutions): null rays of the static metric
+ *   ds^2 = -a^2 dt^2 + p^4 (dx^2 + dy^2 + dz^2),
+ *   p = 1 + S, a = (1 - S) / (1 + S), S = sum_i m_i / (2 |x - x_i|),
+ * with every position taken as an isotropic coordinate. For one hole this is
+ * Schwarzschild (areal radius r = rho (1 + m / 2 rho)^2); p is the
+ * Brill-Lindquist conformal factor of several holes. Rays follow Fermat's
+ * principle with index n = p^2 / a, integrated by RK4 in Euclidean arc
+ * length with step `step` times the distance to the nearest hole. A ray is
+ * captured where S reaches 0.9, escapes through the sphere of radius
+ * r_escape * (sum of masses) about the holes' centre of mass, and is tested
+ * against the disc (the curved step, Hermite-interpolated) and the objects
+ * (the step's chord) on every step (GRID schedule, FP32 or FP64). */
+enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1, BH_INTEGRATOR_FLAT = 2, BH_INTEGRATOR_MULTI = 3 };
 
 /* Arithmetic. MIXED (RK4 only): FP32 bulk, FP64 for rays whose impact
  * parameter lies within `band` of 3*sqrt(3)*M, FP64 disc-crossing refinement. */
@@ -128,6 +142,8 @@ typedef struct bh_object {
 
 /* Objects per scene accepted by the render calls. */
 #define BH_MAX_OBJECTS 64
+/* Holes per scene (the scene's hole and its extra holes) of the MULTI integrator. */
+#define BH_MAX_HOLES 8
 
 /* ---- scene ------------------------------------------------------------------ */
 /* Camera<T> state (camera.h:21-71 on Object<T>, object/object.h:23-118). */
@@ -174,6 +190,11 @@ typedef struct bh_scene {
                           n_objects is 0. Objects need the GRID schedule and
                           FP32 or FP64 (not MIXED), and no differentiable
                           render. */
+  int32_t n_extra_holes; /* entries of `extra_holes` (0..BH_MAX_HOLES - 1);
+                          non-zero only with the MULTI integrator */
+  int32_t reserved_holes;
+  const bh_hole* extra_holes; /* host memory, read during the call; NULL when
+                          n_extra_holes is 0 */
 } bh_scene;
 
 /* One output frame; width and height come from the scene's camera. */
@@ -182,8 +203,12 @@ typedef struct bh_frame {
   uint8_t* hit_class;  /* optional (NULL): width*height BH_CLASS_* */
   float* aux;          /* optional (NULL): width*height. RK4: deflection
                           angle (rad) of escaped rays, hit radius (units of M)
-                          of disc hits; RK4 and FLAT: the object's index of
-                          object hits; 0 otherwise (not REF_TRAPEZOID) */
+                          of disc hits; MULTI: the angle (rad) between the
+                          ray's first and last direction of escaped rays, the
+                          hit's distance from the disc centre (units of the
+                          scene hole's mass) of disc hits; RK4, MULTI and
+                          FLAT: the object's index of object hits; 0
+                          otherwise (not REF_TRAPEZOID) */
 } bh_frame;
 
 typedef struct bh_render_options {
@@ -192,9 +217,11 @@ typedef struct bh_render_options {
   int32_t raygen;            /* BH_RAYGEN_* (default REF) */
   int32_t format;            /* BH_FORMAT_* (default BGRA8) */
   int32_t schedule;          /* BH_SCHEDULE_* (default GRID) */
-  int32_t max_steps;         /* RK4 step cap (default 4000) */
-  double step;               /* RK4 step in phi (default 0.01) */
-  double r_escape;           /* RK4 escape radius in units of M (default 100) */
+  int32_t max_steps;         /* RK4 / MULTI step cap (default 4000) */
+  double step;               /* RK4 step in phi (default 0.01); MULTI: step
+                                length per unit distance to the nearest hole */
+  double r_escape;           /* RK4 escape radius in units of M (default 100);
+                                MULTI: in units of the holes' total mass */
   double band;               /* MIXED: rays with |b - 3 sqrt(3) M| < band * M are
                                 traced in FP64 with step band_step (default 5e-4) */
   int32_t block_x;           /* GRID block shape (default 32 x 4) */

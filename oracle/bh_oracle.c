@@ -32,6 +32,10 @@
  *     drives it: ten chords from the focus through the PixelVector point,
  *     the step scaled by 100 / |step|^2 when |step|^2 < 100.
  *
+ *   orc_render_multi -- the MULTI integrator (several holes; see
+ *     multi_pixel below): no counterpart in the reference to restate, its
+ *     multi-hole experiment being disabled and unfinished.
+ *
  *   Ordinary objects (bh_object) take part in every chord test of modes A
  *   and flat, and of each RK4 step of mode B: Rectangle::Collide / color
  *   (vector_object.h:107-180), Triangle::Collide (:39-71, black),
@@ -143,6 +147,11 @@ typedef struct {
   int n_obj;
   const bh_object* obj;
   const orc_texture* obj_tex; /* one per object (NULL bgra: none), or NULL */
+  int n_holes;                /* MULTI: the scene's hole, then its extra holes */
+  vec3 hp[BH_MAX_HOLES];
+  double hm[BH_MAX_HOLES];    /* half of each mass */
+  vec3 mcen;                  /* centre of mass */
+  double mtot;
 } view;
 
 static void make_view(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* bg_tex, view* v) {
@@ -174,6 +183,17 @@ static void make_view(const bh_scene* s, const orc_texture* disc_tex, const orc_
   if (v->has_bg) v->bg_tex = *bg_tex;
   v->n_obj = s->n_objects;
   v->obj = s->objects;
+  v->n_holes = 1 + (s->n_extra_holes > 0 ? s->n_extra_holes : 0);
+  v->mcen = v3(0, 0, 0);
+  v->mtot = 0;
+  for (int i = 0; i < v->n_holes; ++i) {
+    const bh_hole* h = i == 0 ? &s->hole : &s->extra_holes[i - 1];
+    v->hp[i] = v3a(h->position);
+    v->hm[i] = 0.5 * h->mass;
+    v->mtot += h->mass;
+    v->mcen = add(v->mcen, scale(v->hp[i], h->mass));
+  }
+  v->mcen = scale(v->mcen, 1.0 / v->mtot);
 }
 
 /* Camera::focus_vector / PixelVector(x, y, fv), camera.h:55-63 */
@@ -776,6 +796,168 @@ static int flat_pixel(const view* v, int x, int y, uint8_t out[4], int* obj) {
   return BH_CLASS_MISS;
 }
 
+/* MULTI: null rays of ds^2 = -a^2 dt^2 + p^4 |dx|^2 with p = 1 + S,
+ * a = (1 - S) / (1 + S), S = sum m_i / (2 |x - x_i|) (isotropic coordinates;
+ * one hole: Schwarzschild). Their spatial paths are the rays of the index
+ * n = (1 + S)^3 / (1 - S): dx/ds = T, dT/ds = g - T (T . g), g = grad ln n.
+ * RK4 in the Euclidean arc length s with h = step * (distance to the nearest
+ * hole); capture at S >= 0.9; escape through the sphere of radius
+ * r_escape * (total mass) about the centre of mass, moving outward; per step
+ * the disc on the Hermite curve of the step (three Newton steps from the
+ * chord's estimate) and the objects on its chord, the earlier winning (the
+ * disc on ties). aux: the angle between the first and the last direction of
+ * an escaped ray, the distance of a disc hit from the disc centre / m_0, the
+ * index of an object hit. No counterpart in the reference, whose
+ * multiple_blackhole_solution_test.cc:149-262 averages per-hole plane
+ * solutions. */
+typedef struct {
+  vec3 a;
+  double S, d2;
+} meval;
+
+static meval multi_eval(const view* v, vec3 x, vec3 T) {
+  double S = 0, d2 = 1e300;
+  vec3 gS = v3(0, 0, 0);
+  for (int i = 0; i < v->n_holes; ++i) {
+    vec3 d = sub(x, v->hp[i]);
+    double r2 = dot(d, d);
+    double ir = 1.0 / sqrt(r2);
+    double k = v->hm[i] * ir;
+    S += k;
+    gS = sub(gS, scale(d, k * ir * ir));
+    if (r2 < d2) d2 = r2;
+  }
+  double f = 3.0 / (1.0 + S) + 1.0 / (1.0 - S);
+  vec3 g = scale(gS, f);
+  meval e;
+  e.a = sub(g, scale(T, dot(T, g)));
+  e.S = S;
+  e.d2 = d2;
+  return e;
+}
+
+static void hermite3(vec3 x0, vec3 m0, vec3 x1, vec3 m1, double t, vec3* p, vec3* dp) {
+  double t2 = t * t, t3 = t2 * t;
+  *p = add(add(scale(x0, 2 * t3 - 3 * t2 + 1), scale(m0, t3 - 2 * t2 + t)),
+           add(scale(x1, 3 * t2 - 2 * t3), scale(m1, t3 - t2)));
+  *dp = add(add(scale(x0, 6 * t2 - 6 * t), scale(m0, 3 * t2 - 4 * t + 1)),
+            add(scale(x1, 6 * t - 6 * t2), scale(m1, 3 * t2 - 2 * t)));
+}
+
+static double clamp01(double t) { return t < 0 ? 0 : (t > 1 ? 1 : t); }
+
+static void multi_pixel(const view* v, const orc_rk4_opts* o, int x, int y, rk4_result* res) {
+  memset(res, 0, sizeof(*res));
+  res->bgra[3] = 255;
+  res->margin_tex = 1.0;
+  res->margin_r = 1e30;
+  vec3 fv = scale(v->vx, v->focus_len);
+  vec3 pv = pixel_vector(v, x, y, fv); /* a point, as the reference uses it */
+  const vec3 T0 = normalize(sub(pv, v->focus));
+  const double resc = o->r_escape * v->mtot;
+  vec3 X = v->focus, T = T0;
+  meval e = multi_eval(v, X, T);
+  {
+    vec3 F = sub(v->focus, v->hp[0]);
+    double n = pow(1 + e.S, 3) / (1 - e.S);
+    res->b_over_m = n * sqrt(dot(cross(F, T0), cross(F, T0))) / (2 * v->hm[0]);
+  }
+  res->cls = BH_CLASS_MAXSTEPS;
+  int k = 0;
+  for (;; ++k) {
+    if (e.S >= 0.9) {
+      res->cls = BH_CLASS_HORIZON;
+      break;
+    }
+    if (k >= o->max_steps) break;
+    double h = o->step * sqrt(e.d2), hh = 0.5 * h;
+    vec3 t2 = add(T, scale(e.a, hh));
+    meval e2 = multi_eval(v, add(X, scale(T, hh)), t2);
+    vec3 t3 = add(T, scale(e2.a, hh));
+    meval e3 = multi_eval(v, add(X, scale(t2, hh)), t3);
+    vec3 t4 = add(T, scale(e3.a, h));
+    meval e4 = multi_eval(v, add(X, scale(t3, h)), t4);
+    double h6 = h / 6.0;
+    vec3 Xn = add(X, scale(add(add(T, scale(add(t2, t3), 2.0)), t4), h6));
+    vec3 Tn = normalize(add(T, scale(add(add(e.a, scale(add(e2.a, e3.a), 2.0)), e4.a), h6)));
+    double f_disc = 2;
+    vec3 dhit = v3(0, 0, 0);
+    if (v->disc_on) {
+      double g0 = dot(v->dnorm, sub(X, v->dcen)), g1 = dot(v->dnorm, sub(Xn, v->dcen));
+      if ((g0 > 0) != (g1 > 0)) {
+        double t = g0 != g1 ? g0 / (g0 - g1) : 0.5;
+        vec3 p, dp;
+        for (int i = 0; i < 3; ++i) {
+          hermite3(X, scale(T, h), Xn, scale(Tn, h), t, &p, &dp);
+          double dd = dot(v->dnorm, dp);
+          if (dd != 0) t = clamp01(t - dot(v->dnorm, sub(p, v->dcen)) / dd);
+        }
+        hermite3(X, scale(T, h), Xn, scale(Tn, h), t, &p, &dp);
+        vec3 q = sub(p, v->dcen);
+        double rr = sqrt(dot(q, q));
+        if (rr >= v->r_in && rr <= v->r_out) {
+          f_disc = t;
+          dhit = p;
+        }
+      }
+    }
+    double f_obj = 2;
+    int obj = -1;
+    vec3 ohit = v3(0, 0, 0);
+    if (v->n_obj > 0) {
+      double dd = 0;
+      obj = nearest_object(v, X, Xn, &dd, &ohit);
+      if (obj >= 0) {
+        vec3 ch = sub(Xn, X);
+        f_obj = sqrt(dd / dot(ch, ch));
+      }
+    }
+    if (f_disc <= 1 && f_disc <= f_obj) {
+      vec3 q = sub(dhit, v->dcen);
+      double rr = sqrt(dot(q, q));
+      res->cls = BH_CLASS_DISC;
+      res->aux = rr / (2 * v->hm[0]);
+      double dr1 = rr - v->r_in, dr2 = v->r_out - rr;
+      res->margin_r = (dr1 < dr2 ? dr1 : dr2) / (2 * v->hm[0]);
+      color_disc(v, dhit, res->bgra, &res->margin_tex);
+      ++k;
+      break;
+    }
+    if (f_obj <= 1) {
+      res->cls = BH_CLASS_OBJECT;
+      res->aux = obj;
+      color_object(v, obj, ohit, res->bgra);
+      ++k;
+      break;
+    }
+    vec3 q = sub(Xn, v->mcen);
+    if (dot(q, q) >= resc * resc && dot(Tn, q) > 0) {
+      vec3 q0 = sub(X, v->mcen);
+      double r0 = sqrt(dot(q0, q0)), r1 = sqrt(dot(q, q));
+      double t = r1 != r0 ? clamp01((resc - r0) / (r1 - r0)) : 1.0;
+      vec3 p, dp;
+      for (int i = 0; i < 3; ++i) {
+        hermite3(X, scale(T, h), Xn, scale(Tn, h), t, &p, &dp);
+        vec3 w = sub(p, v->mcen);
+        double dd = 2 * dot(w, dp);
+        if (dd != 0) t = clamp01(t - (dot(w, w) - resc * resc) / dd);
+      }
+      hermite3(X, scale(T, h), Xn, scale(Tn, h), t, &p, &dp);
+      vec3 Te = normalize(dp);
+      vec3 cr = cross(T0, Te);
+      res->cls = BH_CLASS_MISS;
+      res->aux = atan2(sqrt(dot(cr, cr)), dot(T0, Te));
+      if (v->has_bg) color_background(v, Te, res->bgra, &res->margin_tex);
+      ++k;
+      break;
+    }
+    X = Xn;
+    T = Tn;
+    e = multi_eval(v, X, T);
+  }
+  res->steps = k;
+}
+
 /* ------------------------------------------------------------------------- */
 static void set_threads(int nthreads) {
 #ifdef _OPENMP
@@ -853,6 +1035,32 @@ int orc_render_flat(const bh_scene* s, const orc_texture* disc_tex, const orc_te
     if (out->bgra) memcpy(out->bgra + 4 * i, c, 4);
     if (out->cls) out->cls[i] = (uint8_t)cls;
     if (out->aux) out->aux[i] = obj;
+  }
+  return 0;
+}
+
+/* MULTI over the whole image or a pixel list (REF ray generation). */
+int orc_render_multi(const bh_scene* s, const orc_texture* disc_tex, const orc_texture* bg_tex,
+                     const orc_texture* obj_tex, const orc_rk4_opts* o, const int32_t* pixels, int64_t npix,
+                     const orc_outputs* out, int nthreads) {
+  view v;
+  make_view(s, disc_tex, bg_tex, &v);
+  v.obj_tex = obj_tex;
+  const int64_t n = pixels ? npix : (int64_t)v.W * v.H;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) {
+    int x = pixels ? pixels[2 * i] : (int)(i % v.W);
+    int y = pixels ? pixels[2 * i + 1] : (int)(i / v.W);
+    rk4_result r;
+    multi_pixel(&v, o, x, y, &r);
+    if (out->bgra) memcpy(out->bgra + 4 * i, r.bgra, 4);
+    if (out->cls) out->cls[i] = (uint8_t)r.cls;
+    if (out->aux) out->aux[i] = r.aux;
+    if (out->margin_tex) out->margin_tex[i] = r.margin_tex;
+    if (out->margin_r) out->margin_r[i] = r.margin_r;
+    if (out->b_over_m) out->b_over_m[i] = r.b_over_m;
+    if (out->steps) out->steps[i] = r.steps;
   }
   return 0;
 }

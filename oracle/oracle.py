@@ -70,6 +70,8 @@ def load():
         lib.orc_render_rk4.argtypes = [C.c_void_p, C.POINTER(OrcTexture), C.POINTER(OrcTexture),
                                        C.POINTER(OrcTexture), C.POINTER(OrcRk4Opts), C.c_void_p, C.c_int64,
                                        C.POINTER(OrcOutputs), C.c_int]
+        lib.orc_render_multi.restype = C.c_int
+        lib.orc_render_multi.argtypes = lib.orc_render_rk4.argtypes
         lib.orc_max_threads.restype = C.c_int
         _lib = lib
     return _lib
@@ -138,8 +140,10 @@ def render_ref(scene, pixels=None, threads: int = 0) -> dict:
 
 
 def render_rk4(scene, step: float = 0.01, max_steps: int = 4000, r_escape: float = 100.0, pixels=None,
-               threads: int = 0) -> dict:
-    """Oracle B: RK4 in phi, FP64."""
+               threads: int = 0, multi: bool = False) -> dict:
+    """Oracle B: RK4 in phi, FP64 (multi: the MULTI integrator's RK4 in arc
+    length over the scene's hole and extra holes; step is its factor on the
+    distance to the nearest hole, r_escape in units of the total mass)."""
     lib = load()
     s = _scene_c(scene)
     dt, dta = _tex(scene.disc.texture if scene.disc is not None else None)
@@ -156,12 +160,19 @@ def render_rk4(scene, step: float = 0.01, max_steps: int = 4000, r_escape: float
                                                     "steps")))
     opts = OrcRk4Opts(step, max_steps, r_escape)
     ot, otk = _obj_tex(scene)
-    lib.orc_render_rk4(C.byref(s), C.byref(dt) if dt else None, C.byref(bt) if bt else None, ot, C.byref(opts),
-                       pp, n, C.byref(out), threads)
+    fn = lib.orc_render_multi if multi else lib.orc_render_rk4
+    fn(C.byref(s), C.byref(dt) if dt else None, C.byref(bt) if bt else None, ot, C.byref(opts), pp, n, C.byref(out),
+       threads)
     if pixels is None:
         h, w = scene.camera.height(), scene.camera.width()
         res = {k: v.reshape((h, w) + v.shape[1:]) for k, v in res.items()}
     return res
+
+
+def render_multi(scene, step: float = 0.01, max_steps: int = 4000, r_escape: float = 100.0, pixels=None,
+                 threads: int = 0) -> dict:
+    """The MULTI integrator, FP64 (REF ray generation)."""
+    return render_rk4(scene, step, max_steps, r_escape, pixels, threads, multi=True)
 
 
 def render_flat(scene, pixels=None, threads: int = 0) -> dict:

@@ -35,7 +35,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.bh_abi_version() == capi.ABI_VERSION == 2
+    assert lib.bh_abi_version() == capi.ABI_VERSION == 3
     o = capi.default_options()
     assert o.integrator == capi.INTEGRATOR_RK4 and o.step == 0.01 and o.max_steps == 4000
     assert o.r_escape == 100.0 and o.block_x * o.block_y % 32 == 0
@@ -54,6 +54,8 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu\n", offsetof(bh_render_options, step), offsetof(bh_render_options, band),
          offsetof(bh_render_options, refill_threshold), offsetof(bh_render_options, band_lanes),
          offsetof(bh_render_options, band_serial));
+  printf("%zu %zu %zu %d %d\n", offsetof(bh_scene, objects), offsetof(bh_scene, n_extra_holes),
+         offsetof(bh_scene, extra_holes), BH_MAX_HOLES, BH_INTEGRATOR_MULTI);
   return 0;
 }
 ''')
@@ -68,6 +70,8 @@ int main(void) {
     assert offs == [capi.RenderOptions.step.offset, capi.RenderOptions.band.offset,
                     capi.RenderOptions.refill_threshold.offset, capi.RenderOptions.band_lanes.offset,
                     capi.RenderOptions.band_serial.offset]
+    assert list(map(int, out[2].split())) == [capi.Scene.objects.offset, capi.Scene.n_extra_holes.offset,
+                                              capi.Scene.extra_holes.offset, capi.MAX_HOLES, capi.INTEGRATOR_MULTI]
 
 
 def test_create_without_device_reports_no_device(lib):
