@@ -171,8 +171,74 @@ def run_reference(args):
 
 
 ADJ_SIDE = 512
+MULTI_STEP = 0.02  # MULTI integrator: step per unit distance to the nearest hole
 ADJ_WORKLOAD = "adjoint 512x512: MSE vs target at M+5%, disc tilt +3 deg, r_out +2M, yaw/pitch +1 deg; " \
                "gradient w.r.t. M, camera position and yaw/pitch/roll, disc tilt, r_in, r_out; checkpoints every 64 steps"
+
+
+def time_sequence(r, args, scenes, opts):
+    """Mean device time of K replays (after W) of the scenes captured as one
+    sequence (CUDA graph), CUDA events on the context's stream."""
+    import torch
+
+    from blackhole_8_gb300 import capi
+
+    cs = r.c_scenes(scenes)
+    bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
+            for s in scenes]
+    frames = (capi.Frame * len(scenes))()
+    for i, b in enumerate(bufs):
+        frames[i].pixels = b.data_ptr()
+    seq = r.sequence(cs, frames, opts)
+    stream = torch.cuda.ExternalStream(r.stream)
+    for _ in range(args.warmup):
+        seq.launch()
+    stream.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        seq.launch()
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    st = seq.stats()
+    seq.close()
+    rays = sum(s.camera.width() * s.camera.height() for s in scenes)
+    return {"mrays_per_s": round(rays / (ms * 1e-3) / 1e6, 3), "ms_per_step": round(ms, 3),
+            "steps_per_ray": round(st.steps / max(1, st.rays), 1)}
+
+
+def multi_leg(r, args, cpu: bool):
+    """Times the MULTI integrator (several holes): an equal-mass binary with a
+    circumbinary disc at 8 phases of its orbit, 1920x1080, on the GPU (FP32
+    frames, FP64 the first frame) and its FP64 CPU restatement (the oracle
+    port, all host threads) on a 192x108 sample of the first frame. The
+    reference's own multi-hole code is disabled in its build and does not
+    run, so the CPU figure is the port's."""
+    import time
+
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+
+    frames = S.binary_orbit(8, 1920, 1080)
+    o32 = capi.default_options(integrator=capi.INTEGRATOR_MULTI, step=MULTI_STEP, max_steps=20000)
+    o64 = capi.default_options(integrator=capi.INTEGRATOR_MULTI, precision=capi.PRECISION_FP64, step=MULTI_STEP,
+                               max_steps=20000)
+    out = {"workload": "equal-mass binary (2 x 0.5 M, 6 M apart) + circumbinary disc 8.4-20 M, 8 orbit phases "
+                       f"1920x1080; step {MULTI_STEP} x distance to the nearest hole",
+           "fp32": time_sequence(r, args, frames, o32),
+           "fp64_first_frame": time_sequence(r, args, frames[:1], o64)}
+    if cpu:
+        from oracle import oracle
+        sample = S.binary_orbit(8, 192, 108)[0]
+        threads = oracle.max_threads()
+        oracle.render_multi(sample, step=MULTI_STEP, max_steps=20000, threads=threads)  # warm
+        t0 = time.perf_counter()
+        oracle.render_multi(sample, step=MULTI_STEP, max_steps=20000, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_port"] = {"mrays_per_s": round(192 * 108 / dt / 1e6, 4), "cores": threads, "kind": "port",
+                           "sample": "first frame at 192x108, FP64"}
+    return out
 
 
 def objects_leg(r, args, cpu: bool):
@@ -207,27 +273,7 @@ def objects_leg(r, args, cpu: bool):
         return out
 
     def time_seq(scenes, opts):
-        cs = r.c_scenes(scenes)
-        bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
-                for s in scenes]
-        frames = (capi.Frame * len(scenes))()
-        for i, b in enumerate(bufs):
-            frames[i].pixels = b.data_ptr()
-        seq = r.sequence(cs, frames, opts)
-        stream = torch.cuda.ExternalStream(r.stream)
-        for _ in range(args.warmup):
-            seq.launch()
-        stream.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(args.steps):
-            seq.launch()
-        b.record(stream)
-        b.synchronize()
-        ms = a.elapsed_time(b) / args.steps
-        seq.close()
-        rays = sum(s.camera.width() * s.camera.height() for s in scenes)
-        return {"mrays_per_s": round(rays / (ms * 1e-3) / 1e6, 3), "ms_per_step": round(ms, 3)}
+        return time_sequence(r, args, scenes, opts)
 
     def cpu_ref(scenes, flat):
         if not cpu:
@@ -470,6 +516,7 @@ def run_ours(args):
     objects = None
     if not args.no_objects:
         objects = objects_leg(r, args, cpu=rank == 0 and not args.no_cpu)
+        objects["multi_holes"] = multi_leg(r, args, cpu=rank == 0 and not args.no_cpu)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -21,7 +21,7 @@ import time
 
 PRECISIONS = {"fp32": 0, "fp64": 1, "mixed": 2}
 SCHEDULES = {"grid": 0, "persistent": 1}
-INTEGRATORS = {"ref": 0, "rk4": 1, "flat": 2}
+INTEGRATORS = {"ref": 0, "rk4": 1, "flat": 2, "multi": 3}
 
 
 def build_scenes(args):
@@ -40,6 +40,8 @@ def build_scenes(args):
         return [S.objects_scene(args.width or 640, args.height or 360) for _ in range(args.frames)]
     if args.workload == "flat":
         return [S.flat_demo_scene(args.width or 800, args.height or 450) for _ in range(args.frames)]
+    if args.workload == "binary":
+        return S.binary_orbit(args.frames, args.width or 1920, args.height or 1080)
     raise SystemExit(f"unknown workload {args.workload}")
 
 
@@ -53,7 +55,8 @@ def write_ppm(path: str, bgra) -> None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--workload", default="flythrough",
-                    choices=["single", "flythrough", "batched", "photon-ring", "adjoint", "objects", "flat"])
+                    choices=["single", "flythrough", "batched", "photon-ring", "adjoint", "objects", "flat",
+                             "binary"])
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)

@@ -561,6 +561,23 @@ def binary_scene(width: int = 640, height: int = 360, seed: int = 0, separation:
                  {"workload": f"binary {width}x{height}"}, extra_holes=[h2])
 
 
+def binary_orbit(frames: int = 8, width: int = 1920, height: int = 1080, seed: int = 0,
+                 separation: float = 6.0) -> list[Scene]:
+    """The equal-mass binary_scene at `frames` phases of one orbit: the holes
+    turned about the disc normal by 2 pi k / frames."""
+    out = []
+    for k in range(frames):
+        sc = binary_scene(width, height, seed, separation)
+        a = 2 * math.pi * k / frames
+        c, s = math.cos(a), math.sin(a)
+        for h in [sc.hole] + sc.extra_holes:
+            x, y, z = h.position()
+            h.MoveTo(c * x - s * y, s * x + c * y, z)
+        sc.meta = {"workload": f"binary orbit {width}x{height}", "frame": k}
+        out.append(sc)
+    return out
+
+
 def panel_texture(seed: int, width: int = 160, height: int = 120) -> Texture:
     """A hash-noise BGR8 picture for a Rectangle (no black texels)."""
     def make():

@@ -446,6 +446,7 @@ struct Scene {
   const Annulus<T>* disc = nullptr;          // may be null
   const Background* background = nullptr;    // may be null
   std::vector<SceneObject<T>> objects;
+  std::vector<const StaticBlackhole<T>*> extra_holes;  // BH_INTEGRATOR_MULTI: holes besides `hole`
 };
 
 template <typename T>
@@ -544,7 +545,7 @@ class Renderer {
   template <typename T>
   void Render(const Camera<T>& cam, const StaticBlackhole<T>& bh, const Annulus<T>* disc, const Background* bg,
               Image& out, const Options& opts = Options()) {
-    std::vector<Scene<T>> one{Scene<T>{&cam, &bh, disc, bg, {}}};
+    std::vector<Scene<T>> one{Scene<T>{&cam, &bh, disc, bg, {}, {}}};
     std::vector<Image> imgs(1);
     Render(one, imgs, opts);
     out = std::move(imgs[0]);
@@ -554,8 +555,8 @@ class Renderer {
   // opts.schedule is BH_SCHEDULE_PERSISTENT).
   template <typename T>
   void Render(const std::vector<Scene<T>>& scenes, std::vector<Image>& out, const Options& opts = Options()) {
-    std::vector<std::vector<bh_object>> objects;
-    std::vector<bh_scene> pods = Pods(scenes, &objects);
+    PodTables tables;
+    std::vector<bh_scene> pods = Pods(scenes, &tables);
     out.resize(scenes.size());
     std::vector<bh_frame> frames(scenes.size());
     for (size_t i = 0; i < scenes.size(); ++i) {
@@ -578,8 +579,8 @@ class Renderer {
   template <typename T>
   AdjointResult Adjoint(const Scene<T>& scene, const double* theta, const float* d_target, float* d_image = nullptr,
                         float* d_pixel_grad = nullptr, const bh_adjoint_options* opts = nullptr) {
-    std::vector<std::vector<bh_object>> objects;
-    std::vector<bh_scene> pods = Pods(std::vector<Scene<T>>{scene}, &objects);
+    PodTables tables;
+    std::vector<bh_scene> pods = Pods(std::vector<Scene<T>>{scene}, &tables);
     bh_adjoint_frame fr{d_target, d_image, d_pixel_grad};
     bh_adjoint_result r;
     Check(bh_render_adjoint(ctx_, pods.data(), 1, theta, &fr, opts, &r), "bh_render_adjoint");
@@ -612,12 +613,19 @@ class Renderer {
     return id;
   }
 
-  // The scenes' PODs; `objects` holds their object tables during the call.
+  // The object and extra-hole tables the PODs point at, kept during a call.
+  struct PodTables {
+    std::vector<std::vector<bh_object>> objects;
+    std::vector<std::vector<bh_hole>> holes;
+  };
+
+  // The scenes' PODs; `tables` holds their object and hole tables.
   template <typename T>
-  std::vector<bh_scene> Pods(const std::vector<Scene<T>>& scenes, std::vector<std::vector<bh_object>>* objects) {
+  std::vector<bh_scene> Pods(const std::vector<Scene<T>>& scenes, PodTables* tables) {
     std::vector<bh_scene> pods;
     pods.reserve(scenes.size());
-    objects->assign(scenes.size(), {});
+    tables->objects.assign(scenes.size(), {});
+    tables->holes.assign(scenes.size(), {});
     const StaticBlackhole<T> no_hole(typename Object<T>::point_type(0, 0, 0), T(1));  // FLAT ignores the hole
     for (size_t i = 0; i < scenes.size(); ++i) {
       const Scene<T>& s = scenes[i];
@@ -629,7 +637,7 @@ class Renderer {
       }
       if (s.background) bt = TextureId(s.background->texture());
       bh_scene pod = ToPod(*s.camera, s.hole ? *s.hole : no_hole, s.disc, dt, bt);
-      auto& tab = (*objects)[i];
+      auto& tab = tables->objects[i];
       for (const SceneObject<T>& so : s.objects) {
         int32_t tex = -1;
         if (so.rectangle && !so.rectangle->texture().empty()) tex = TextureId(so.rectangle->texture());
@@ -637,6 +645,16 @@ class Renderer {
       }
       pod.n_objects = int32_t(tab.size());
       pod.objects = tab.empty() ? nullptr : tab.data();
+      auto& holes = tables->holes[i];
+      for (const StaticBlackhole<T>* h : s.extra_holes) {
+        if (!h) throw Error(BH_ERR_INVALID_ARGUMENT, "null extra hole");
+        bh_hole b;
+        copy3(b.position, h->position());
+        b.mass = double(h->mass());
+        holes.push_back(b);
+      }
+      pod.n_extra_holes = int32_t(holes.size());
+      pod.extra_holes = holes.empty() ? nullptr : holes.data();
       pods.push_back(pod);
     }
     return pods;

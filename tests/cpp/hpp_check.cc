@@ -9,6 +9,10 @@
 //                                 renders the scene (disc RGBA8 1024x64 and sky
 //                                 RGB8 2048x1024 texels read from files) and
 //                                 writes BGR24 pixels then hit classes to OUT
+//   hpp_check binary W H DISC BG OUT
+//                                 the same for the equal-mass binary (two holes
+//                                 of mass 1/2 at y = -+3, disc 8.4-20, camera at
+//                                 30 from the origin) with the MULTI integrator
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -122,6 +126,36 @@ int main(int argc, char** argv) {
     // a second render reuses the uploaded textures
     Image again = Render(b.cam, b.bh, &b.disc, &sky, o);
     if (again.pixels != img.pixels) return fail("repeat render differs");
+    std::ofstream f(argv[6], std::ios::binary);
+    f.write(reinterpret_cast<const char*>(img.pixels.data()), std::streamsize(img.pixels.size()));
+    f.write(reinterpret_cast<const char*>(img.hit_class.data()), std::streamsize(img.hit_class.size()));
+    std::printf("ok %d %d\n", img.width, img.height);
+    return 0;
+  }
+  if (mode == "binary" && argc == 7) {
+    const int w = std::atoi(argv[2]), h = std::atoi(argv[3]);
+    const double incl = 80 * M_PI / 180, r = 30;
+    Camera<double> cam(w, h, 60 * M_PI / 180);
+    cam.RotateZ(-0.0);
+    cam.RotateY(incl - M_PI / 2);
+    cam.MoveTo(-r * std::sin(incl), -0.0, r * std::cos(incl));
+    StaticBlackhole<double> h1({0, -3, 0}, 0.5), h2({0, 3, 0}, 0.5);
+    Annulus<double> disc({20, 20, 0}, {-20, 20, 0}, {-20, -20, 0}, {20, -20, 0}, 20, 1.4 * 6.0);
+    disc.mapping(BH_DISC_MAP_POLAR);
+    const std::vector<uint8_t> dt = read_file(argv[4]), bt = read_file(argv[5]);
+    if (dt.size() != 1024 * 64 * 4 || bt.size() != 2048 * 1024 * 3) return fail("texture files");
+    disc.SetTexture(Texture::FromPixels(1024, 64, BH_TEXEL_RGBA8, dt.data()));
+    Background sky(Texture::FromPixels(2048, 1024, BH_TEXEL_RGB8, bt.data()));
+    Scene<double> sc{&cam, &h1, &disc, &sky, {}, {&h2}};
+    Options o;
+    o.want_classes = true;
+    o.integrator = BH_INTEGRATOR_MULTI;
+    o.precision = BH_PRECISION_FP64;
+    o.step = 0.02;
+    o.max_steps = 20000;
+    std::vector<Image> imgs;
+    DefaultRenderer().Render(std::vector<Scene<double>>{sc}, imgs, o);
+    const Image& img = imgs[0];
     std::ofstream f(argv[6], std::ios::binary);
     f.write(reinterpret_cast<const char*>(img.pixels.data()), std::streamsize(img.pixels.size()));
     f.write(reinterpret_cast<const char*>(img.hit_class.data()), std::streamsize(img.hit_class.size()));

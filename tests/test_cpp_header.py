@@ -115,3 +115,25 @@ def test_cpp_render_matches_python(exe, tmp_path, renderer):
     assert np.array_equal(cls, ref.hit_class)
     orc = oracle.render_rk4(sc)
     assert (cls == orc["cls"]).mean() > 0.999
+
+
+@pytest.mark.gpu
+def test_cpp_binary_render_matches_python(exe, tmp_path, renderer):
+    """Two holes through the C++ layer's Scene::extra_holes and the MULTI
+    integrator: the same frame as the Python mirror's binary scene."""
+    w, h = 64, 36
+    sc = S.binary_scene(w, h)
+    sc.disc.texture.texels.tofile(tmp_path / "disc.raw")
+    sc.background.texels.tofile(tmp_path / "bg.raw")
+    out = subprocess.run([exe, "binary", str(w), str(h), str(tmp_path / "disc.raw"), str(tmp_path / "bg.raw"),
+                          str(tmp_path / "out.raw")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    raw = np.fromfile(tmp_path / "out.raw", dtype=np.uint8)
+    px = raw[:w * h * 3].reshape(h, w, 3)
+    cls = raw[w * h * 3:].reshape(h, w)
+    ref = renderer.render([sc], capi.default_options(integrator=capi.INTEGRATOR_MULTI, precision=capi.PRECISION_FP64,
+                                                     step=0.02, max_steps=20000, format=capi.FORMAT_BGR8),
+                          hit_class=True)[0]
+    assert np.array_equal(px, ref.pixels)
+    assert np.array_equal(cls, ref.hit_class)
+    assert (cls == capi.CLASS_HORIZON).sum() > 0 and (cls == capi.CLASS_DISC).sum() > 0
