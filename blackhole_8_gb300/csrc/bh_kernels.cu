@@ -985,23 +985,53 @@ __device__ __forceinline__ void load_hole<double>(const DevHole& h, V3<double>* 
   *hm = h.hm;
 }
 
+// Reciprocal square root and reciprocal of the MULTI integrator: in FP32 the
+// PTX approximations (rsqrt.approx / rcp.approx, relative error below 2^-22,
+// flush-to-zero: squared distances are at least (m/2)^2 and 1 +- S lies in
+// [0.1, 2] away from the capture), the exact forms in FP64.
+__device__ __forceinline__ float multi_rsqrt(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ double multi_rsqrt(double x) { return 1.0 / sqrt(x); }
+__device__ __forceinline__ float multi_rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ double multi_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float multi_sqrt(float x) { return x * multi_rsqrt(x); }
+__device__ __forceinline__ double multi_sqrt(double x) { return sqrt(x); }
 template <typename R>
+__device__ __forceinline__ V3<R> multi_normalize(V3<R> a) { return a * multi_rsqrt(dot(a, a)); }
+
+// kN: the number of holes when known at compile time (1 or 2), 0 for any.
+template <typename R, int kN>
 __device__ __forceinline__ MultiEval<R> multi_eval(const DevScene& s, V3<R> x, V3<R> T) {
   R S = R(0), d2 = R(3e38);
   V3<R> gS = {R(0), R(0), R(0)};
-  for (int i = 0; i < s.n_holes; ++i) {
+  const int n = kN > 0 ? kN : s.n_holes;
+#pragma unroll
+  for (int i = 0; i < (kN > 0 ? kN : BH_MAX_HOLES); ++i) {
+    if (kN == 0 && i >= n) break;
     V3<R> p;
     R hm;
     load_hole<R>(s.holes[i], &p, &hm);
     const V3<R> d = x - p;
     const R r2 = dot(d, d);
-    const R ir = rnorm(r2);
+    const R ir = multi_rsqrt(r2);
     const R k = hm * ir;
     S += k;
     gS = gS - d * (k * ir * ir);
     d2 = fmin(d2, r2);
   }
-  const R f = shade_div(R(3), R(1) + S) + shade_div(R(1), R(1) - S);
+  R f;
+  if constexpr (sizeof(R) == 4) {
+    f = R(3) * multi_rcp(R(1) + S) + multi_rcp(R(1) - S);
+  } else {
+    f = R(3) / (R(1) + S) + R(1) / (R(1) - S);
+  }
   const V3<R> g = gS * f;
   return {g - T * dot(T, g), S, d2};
 }
@@ -1025,15 +1055,18 @@ __device__ __forceinline__ void hermite3(V3<R> x0, V3<R> m0, V3<R> x1, V3<R> m1,
 // whose S reaches 0.9 is captured; one that leaves the escape sphere moving
 // outward escapes in the direction of the Hermite tangent where the curve
 // meets the sphere (three Newton steps).
-template <typename R>
-__device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>& c, int* steps) {
+template <typename R, int kN>
+__device__ Hit trace_multi_n(const DevScene& s, int px, int py, const Rk4Consts<R>& c, int* steps) {
   const R a_ = BH_S(R, s, half_w) - R(px);
   const R c_ = BH_S(R, s, half_h) - R(py);
   const V3<R> T0 = normalize(BH_V(R, s, E0) + BH_V(R, s, vy) * a_ + BH_V(R, s, vz) * c_) * R(-1);
   const V3<R> cen = BH_V(R, s, mcen);
-  const R resc = BH_S(R, s, r_esc);
+  const R resc = BH_S(R, s, r_esc), resc2 = resc * resc;
+  const bool disc_on = s.disc_on != 0;
+  const V3<R> dn = BH_V(R, s, dn), dc = BH_V(R, s, dc);
+  const R r_in = BH_S(R, s, r_in), r_out = BH_S(R, s, r_out);
   V3<R> X = BH_V(R, s, F), T = T0;
-  MultiEval<R> e = multi_eval<R>(s, X, T);
+  MultiEval<R> e = multi_eval<R, kN>(s, X, T);
   Hit hit = {make_uchar4(0, 0, 0, 255), BH_CLASS_MAXSTEPS, 0.f};
   int k = 0;
   for (;; ++k) {
@@ -1042,21 +1075,20 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
       break;
     }
     if (k >= c.kmax) break;
-    const R h = c.h * sqrt(e.d2), hh = h * R(0.5);
+    const R h = c.h * multi_sqrt(e.d2), hh = h * R(0.5);
     const V3<R> t2 = T + e.a * hh;
-    const MultiEval<R> e2 = multi_eval<R>(s, X + T * hh, t2);
+    const MultiEval<R> e2 = multi_eval<R, kN>(s, X + T * hh, t2);
     const V3<R> t3 = T + e2.a * hh;
-    const MultiEval<R> e3 = multi_eval<R>(s, X + t2 * hh, t3);
+    const MultiEval<R> e3 = multi_eval<R, kN>(s, X + t2 * hh, t3);
     const V3<R> t4 = T + e3.a * h;
-    const MultiEval<R> e4 = multi_eval<R>(s, X + t3 * h, t4);
+    const MultiEval<R> e4 = multi_eval<R, kN>(s, X + t3 * h, t4);
     const R h6 = h * R(1.0 / 6.0);
     const V3<R> Xn = X + (T + (t2 + t3) * R(2) + t4) * h6;
-    const V3<R> Tn = normalize(T + (e.a + (e2.a + e3.a) * R(2) + e4.a) * h6);
+    const V3<R> Tn = multi_normalize(T + (e.a + (e2.a + e3.a) * R(2) + e4.a) * h6);
     // disc crossing on the step's curve
     R f_disc = R(2);
     V3<R> dhit;
-    if (s.disc_on) {
-      const V3<R> dn = BH_V(R, s, dn), dc = BH_V(R, s, dc);
+    if (disc_on) {
       const R g0 = dot(dn, X - dc), g1 = dot(dn, Xn - dc);
       if ((g0 > R(0)) != (g1 > R(0))) {
         R t = g0 != g1 ? shade_div(g0, g0 - g1) : R(0.5);
@@ -1068,7 +1100,7 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
         }
         hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
         const R rr = length(p - dc);
-        if (rr >= BH_S(R, s, r_in) && rr <= BH_S(R, s, r_out)) {
+        if (rr >= r_in && rr <= r_out) {
           f_disc = t;
           dhit = p;
         }
@@ -1091,7 +1123,7 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
     }
     if (f_disc <= R(1) && f_disc <= f_obj) {
       hit.cls = BH_CLASS_DISC;
-      hit.aux = float(length(dhit - BH_V(R, s, dc)) / BH_S(R, s, mass));
+      hit.aux = float(length(dhit - dc) / BH_S(R, s, mass));
       hit.bgra = disc_color(s, dhit);
       ++k;
       break;
@@ -1102,7 +1134,7 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
       break;
     }
     const V3<R> q = Xn - cen;
-    if (dot(q, q) >= resc * resc && dot(Tn, q) > R(0)) {
+    if (dot(q, q) >= resc2 && dot(Tn, q) > R(0)) {
       // the curve meets the escape sphere: |p(t) - cen|^2 = resc^2
       const V3<R> q0 = X - cen;
       const R r0 = length(q0), r1 = length(q);
@@ -1112,7 +1144,7 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
         hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
         const V3<R> w = p - cen;
         const R dd = R(2) * dot(w, dp);
-        if (dd != R(0)) t = fmin(fmax(t - shade_div(dot(w, w) - resc * resc, dd), R(0)), R(1));
+        if (dd != R(0)) t = fmin(fmax(t - shade_div(dot(w, w) - resc2, dd), R(0)), R(1));
       }
       hermite3<R>(X, T * h, Xn, Tn * h, t, &p, &dp);
       const V3<R> Te = normalize(dp);
@@ -1124,10 +1156,19 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
     }
     X = Xn;
     T = Tn;
-    e = multi_eval<R>(s, X, T);
+    e = multi_eval<R, kN>(s, X, T);
   }
   *steps = k;
   return hit;
+}
+
+// The hole count is the same for every ray of a scene: one and two holes
+// get their own unrolled copy.
+template <typename R>
+__device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>& c, int* steps) {
+  if (s.n_holes == 2) return trace_multi_n<R, 2>(s, px, py, c, steps);
+  if (s.n_holes == 1) return trace_multi_n<R, 1>(s, px, py, c, steps);
+  return trace_multi_n<R, 0>(s, px, py, c, steps);
 }
 
 // FP64 trace of a band ray (out of line: keeps FP64 register pressure away
