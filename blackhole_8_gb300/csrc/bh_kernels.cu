@@ -920,9 +920,9 @@ __device__ Hit trace_rk4_obj(const DevScene& s, int x, int y, const Rk4Consts<R>
     R f_obj = R(2);
     Hit ho;
     if (un > R(0)) {
-      const R rn = M / un;
+      const R rn = shade_div(M, un);
       R sp, cp;
-      sincos(R(k + 1) * c.h, &sp, &cp);
+      shade_sincos(R(k + 1) * c.h, &sp, &cp);
       const V3<R> next = BH_V(R, s, Fhat) * (rn * cp) + st.xv * (rn * sp);
       V3<R> hp;
       R bd = R(0);
