@@ -1477,6 +1477,7 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
   long long pend_base = 0;  // first item index of the pending chunk
   unsigned pend_mask = 0;   // its items not yet handed out
   int pend_scene = 0;
+  long long scene_end = 0;  // first ray after pend_scene (FP32 pass)
   bool exhausted = false;
 
   for (;;) {
@@ -1504,9 +1505,21 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
           const long long left = n_items - pend_base;
           pend_mask = left >= chunk ? usable : ((1u << left) - 1u);
           if constexpr (kPass != 2) {
-            int sc = 0;
-            if (lane == 0) sc = find_scene(p, pend_base);
-            pend_scene = __shfl_sync(kFull, sc, 0);
+            // a warp's chunks come in increasing order: its scene stays or
+            // moves forward, so step from the last one while the next scene
+            // has begun (a search only after a long jump)
+            if (pend_base >= scene_end) {
+              int sc = pend_scene;
+              if (lane == 0) {
+                int hops = 0;
+                while (sc + 1 < p.n_scenes && p.scenes[sc + 1].ray_begin <= pend_base && ++hops < 4) ++sc;
+                if (sc + 1 < p.n_scenes && p.scenes[sc + 1].ray_begin <= pend_base) sc = find_scene(p, pend_base);
+              }
+              pend_scene = __shfl_sync(kFull, sc, 0);
+              long long end = p.total_rays;
+              if (lane == 0 && pend_scene + 1 < p.n_scenes) end = p.scenes[pend_scene + 1].ray_begin;
+              scene_end = __shfl_sync(kFull, end, 0);
+            }
           }
         }
         const int n = min(__popc(idle), __popc(pend_mask));
