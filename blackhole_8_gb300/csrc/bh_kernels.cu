@@ -1539,7 +1539,11 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
             if (take_fp32_ray<kPass == 1>(p, scene, item, st, &px, &py, &steps)) ++rays;
           }
         }
-        for (int i = 0; i < n; ++i) pend_mask &= pend_mask - 1u;  // drop the n lowest items
+        // drop the n lowest items: keep the bits from the (n+1)-th set one up
+        if (n > 0) {
+          const unsigned next = __fns(pend_mask, 0, n + 1);  // 0xffffffff when fewer are set
+          pend_mask = next > 31u ? 0u : pend_mask & ~((1u << next) - 1u);
+        }
         given |= __ballot_sync(kFull, ((idle >> lane) & 1u) && rank < n);
         idle = __ballot_sync(kFull, st.status == kDone) & usable & ~given;
       }
