@@ -79,3 +79,22 @@ def test_noalloc_refuses_oversized_calls():
     rc = lib.bh_render_noalloc(0, many, capi.NOALLOC_MAX_SCENES + 1, textures, 2, mframes, None, None, err,
                                len(err))
     assert rc == capi.BH_ERR_INVALID_ARGUMENT
+
+
+def test_noalloc_refuses_several_holes():
+    """The no-alloc entry traces one hole: the MULTI integrator and extra
+    holes are refused before any device work (no GPU needed)."""
+    lib = capi.load()
+    err = C.create_string_buffer(512)
+    sc = S.binary_scene(32, 18)
+    ids = {id(sc.disc.texture): 0, id(sc.background): 1}
+    textures = (capi.DeviceTexture * 2)(capi.DeviceTexture(1, 1024, 64), capi.DeviceTexture(1, 2048, 1024))
+    frames = (capi.Frame * 1)(capi.Frame(1, None, None))
+    cs = (capi.Scene * 1)(sc.to_c(ids))
+    rc = lib.bh_render_noalloc(0, cs, 1, textures, 2, frames, None, None, err, len(err))
+    assert rc == capi.BH_ERR_UNSUPPORTED and b"one hole" in err.value
+    sc.extra_holes = []
+    cs = (capi.Scene * 1)(sc.to_c(ids))
+    opts = capi.default_options(integrator=capi.INTEGRATOR_MULTI)
+    rc = lib.bh_render_noalloc(0, cs, 1, textures, 2, frames, C.byref(opts), None, err, len(err))
+    assert rc == capi.BH_ERR_UNSUPPORTED and b"MULTI" in err.value
