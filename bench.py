@@ -63,6 +63,24 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest x over the ranks of the initialised process group (the
+    step time every rank reports; the job is as slow as its slowest rank)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(rays_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job Mrays/s: every rank renders its own replica of the batch
+    (weak scaling), timed by the slowest rank."""
+    return rays_per_rank * world / seconds / 1e6
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
 
@@ -392,13 +410,6 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     launches = 0
 
@@ -435,7 +446,7 @@ def run_ours(args):
         if seq is not None:
             seq.close()
         launches += kernels_per_step * args.steps
-        return max_over_ranks(ms), st, wall
+        return max_over_ranks(ms, world), st, wall
 
     fp32_tflops, sm_count = r.fp32_peak()
     fp64_tflops = r.fp64_peak()
@@ -464,14 +475,14 @@ def run_ours(args):
         ms, st, wall = time_steps(opts, k, graph)
         fp32_steps = st.steps - st.band_steps
         variants[name] = {"call": "bh_sequence_launch" if graph else "bh_render_device",
-                          "mrays_per_s": round(rays_step * world / (ms * 1e-3) / 1e6, 3),
+                          "mrays_per_s": round(job_throughput(rays_step, world, ms * 1e-3), 3),
                           "ms_per_step": round(ms, 3), "step": opts.step, "steps_total": int(st.steps),
                           "band_rays": int(st.band_rays),
                           "fp32_tflops": round(fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms * 1e-3) / 1e12, 3),
                           "wall_s": round(wall, 3)}
     clock_info = clocks.stop()
 
-    value = rays_step * world / (ms_tuned * 1e-3) / 1e6
+    value = job_throughput(rays_step, world, ms_tuned * 1e-3)
     fp32_steps = st_tuned.steps - st_tuned.band_steps
     # algorithmic flops of the RK4-in-phi steps (50 per step, the orbit's RK4
     # with phi advance, event compares and position recurrence) per second;
@@ -502,10 +513,10 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(args.steps):
             r.render_into(cs, hframes, e2e_opts)
-        dt = max_over_ranks((time.perf_counter() - t0) / args.steps)
+        dt = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
         launches += 5 * args.steps
         st_e2e = r.stats()
-        e2e = {"value": round(rays_step * world / dt / 1e6, 3), "unit": "Mrays/s",
+        e2e = {"value": round(job_throughput(rays_step, world, dt), 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
                "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)", "call": "bh_render"}
 
