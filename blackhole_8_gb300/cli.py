@@ -60,7 +60,8 @@ def main(argv=None) -> int:
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
-    ap.add_argument("--integrator", default="rk4", choices=list(INTEGRATORS))
+    ap.add_argument("--integrator", default=None, choices=list(INTEGRATORS),
+                    help="default: multi for the binary workload, flat for the flat one, rk4 otherwise")
     ap.add_argument("--precision", default="fp32", choices=list(PRECISIONS))
     ap.add_argument("--schedule", default="grid", choices=list(SCHEDULES))
     ap.add_argument("--step", type=float, default=0.01)
@@ -75,6 +76,8 @@ def main(argv=None) -> int:
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ppm", default="")
     args = ap.parse_args(argv)
+    if args.integrator is None:
+        args.integrator = {"binary": "multi", "flat": "flat"}.get(args.workload, "rk4")
 
     import ctypes as C
 

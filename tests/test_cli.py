@@ -47,6 +47,7 @@ def test_workloads_build(workload, n):
     ["--workload", "objects", "--frames", "2"],
     ["--workload", "flat", "--frames", "2", "--integrator", "flat"],
     ["--workload", "binary", "--frames", "2", "--integrator", "multi", "--step", "0.05", "--max-steps", "20000"],
+    ["--workload", "binary", "--frames", "1", "--step", "0.05", "--max-steps", "20000"],  # MULTI by default
 ])
 def test_cli_renders_and_writes_frames(tmp_path, capsys, renderer, argv):
     w, h = 96, 54
@@ -60,7 +61,7 @@ def test_cli_renders_and_writes_frames(tmp_path, capsys, renderer, argv):
     scenes = cli.build_scenes(args)
     kw = {"--integrator": ("integrator", cli.INTEGRATORS), "--precision": ("precision", cli.PRECISIONS),
           "--schedule": ("schedule", cli.SCHEDULES)}
-    opts = {}
+    opts = {"integrator": cli.INTEGRATORS[{"binary": "multi", "flat": "flat"}.get(argv[1], "rk4")]}
     for flag, (name, table) in kw.items():
         if flag in argv:
             opts[name] = table[argv[argv.index(flag) + 1]]
