@@ -669,8 +669,8 @@ void bh_default_options(bh_render_options* o) {
   o->setup_band = 0.1;
   o->slice_steps = 256;
   o->band_lanes = 32;
-  o->block_x = 32;
-  o->block_y = 4;
+  o->block_x = 8;  // each warp an 8 x 4 pixel tile: its rays end closer together than a 32-pixel
+  o->block_y = 16; // row's (measured 4-5 % faster than 32 x 4 on RK4, objects and MULTI renders)
   o->threads_per_block = 256;
   o->blocks_per_sm = 0;
   o->refill_threshold = 32;

@@ -1223,11 +1223,19 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
 
 // ---------------------------------------------------------------------------
 // warp-aggregated counter update
+// The thread's lane in its warp (2-D blocks narrower than 32 threads put
+// several rows of the block in one warp, so threadIdx.x is not the lane).
+__device__ __forceinline__ unsigned lane_id() {
+  unsigned l;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+  return l;
+}
+
 __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
   const unsigned m = __activemask();
   unsigned lo = (unsigned)min(v, 0xffffffffull);
   lo = __reduce_add_sync(m, lo);
-  if ((threadIdx.x & 31) == __ffs(m) - 1 && lo) atomicAdd(dst, (unsigned long long)lo);
+  if (lane_id() == unsigned(__ffs(m) - 1) && lo) atomicAdd(dst, (unsigned long long)lo);
 }
 
 // GRID schedule: one thread per pixel, gridDim.z = scene; one kernel per

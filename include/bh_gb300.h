@@ -224,7 +224,8 @@ typedef struct bh_render_options {
                                 MULTI: in units of the holes' total mass */
   double band;               /* MIXED: rays with |b - 3 sqrt(3) M| < band * M are
                                 traced in FP64 with step band_step (default 5e-4) */
-  int32_t block_x;           /* GRID block shape (default 32 x 4) */
+  int32_t block_x;           /* GRID block shape (default 8 x 16: each warp an
+                                8 x 4 pixel tile) */
   int32_t block_y;
   int32_t threads_per_block; /* PERSISTENT block size (default 256) */
   int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
