@@ -161,3 +161,31 @@ def test_invalid_requests(renderer):
     with pytest.raises(capi.BhError) as e:
         renderer.render([neg], opts())
     assert e.value.code == capi.BH_ERR_INVALID_ARGUMENT
+
+
+def triple_scene(w=96, h=54):
+    """The binary with a third, lighter hole above the disc plane: three
+    holes take the kernel's general (runtime-count) path."""
+    sc = S.binary_scene(w, h)
+    sc.extra_holes.append(S.StaticBlackhole((-2.0, 0.0, 2.5), 0.25))
+    return sc
+
+
+def test_three_holes_match_oracle(renderer):
+    """FP64 through the general hole loop against the restatement. Three
+    holes scatter some rays chaotically, so the bars are robust ones:
+    classes equal on >= 99.5 % and only near boundaries; the bending of
+    escaped rays (the library returns it in FP32) equal to the
+    restatement's rounded to FP32 at the median and within one FP32 ulp
+    of pi at the 99th percentile. (Moving the camera by 1e-13 moves the
+    restatement's bending by at most 5e-13 rad on this scene.)"""
+    sc = triple_scene()
+    o = oracle.render_multi(sc, step=STEP, max_steps=MAX_STEPS)
+    out = renderer.render([sc], opts(precision=capi.PRECISION_FP64), hit_class=True, aux=True)[0]
+    same = out.hit_class == o["cls"]
+    assert same.mean() >= 0.995, same.mean()
+    edge = dilate(helpers.class_boundary_mask(o["cls"]), 2)
+    assert not (~same & ~edge).any(), "class mismatch away from boundaries"
+    esc = same & ~edge & (o["cls"] == capi.CLASS_MISS)
+    err = np.abs(out.aux[esc].astype(np.float64) - o["aux"][esc].astype(np.float32).astype(np.float64))
+    assert np.median(err) == 0.0 and np.percentile(err, 99) <= 2.4e-7, (np.median(err), np.percentile(err, 99))

@@ -106,3 +106,16 @@ def test_binary_mirror_symmetry():
     miss = cls[:, lo:hi] == capi.CLASS_MISS
     assert miss.any() and (cls == capi.CLASS_DISC).any() and (cls == capi.CLASS_HORIZON).any()
     assert np.abs(aux[:, lo:hi] - mirror(aux))[miss].max() < 1e-9
+
+
+def test_third_hole_changes_the_image():
+    """The restatement takes every hole: a third, lighter hole above the
+    binary's disc plane changes classes or bending across the image."""
+    two = S.binary_scene(48, 27)
+    three = S.binary_scene(48, 27)
+    three.extra_holes.append(S.StaticBlackhole((-2.0, 0.0, 2.5), 0.25))
+    a = oracle.render_multi(two, step=0.02, max_steps=20000)
+    b = oracle.render_multi(three, step=0.02, max_steps=20000)
+    changed = (a["cls"] != b["cls"]) | (np.abs(a["aux"] - b["aux"]) > 1e-3)
+    assert changed.mean() > 0.05, changed.mean()
+    assert (b["cls"] == capi.CLASS_HORIZON).sum() > (a["cls"] == capi.CLASS_HORIZON).sum()
