@@ -1000,7 +1000,6 @@ __device__ __forceinline__ float multi_rcp(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
-__device__ __forceinline__ double multi_rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ float multi_sqrt(float x) { return x * multi_rsqrt(x); }
 __device__ __forceinline__ double multi_sqrt(double x) { return sqrt(x); }
 template <typename R>
@@ -1277,12 +1276,6 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   }
 }
 
-template <typename R>
-__device__ __forceinline__ const Rk4Consts<R>& rk4_consts(const LaunchParams& p);
-template <>
-__device__ __forceinline__ const Rk4Consts<float>& rk4_consts<float>(const LaunchParams& p) { return p.c32; }
-template <>
-__device__ __forceinline__ const Rk4Consts<double>& rk4_consts<double>(const LaunchParams& p) { return p.c64; }
 
 // GRID schedule for the FLAT and MULTI integrators and for scenes with objects: one
 // kernel per precision and integrator, so that the object code does not
@@ -1300,13 +1293,13 @@ __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   if (kIntegrator == BH_INTEGRATOR_FLAT) {
     h = trace_flat<R>(s, x, y);
   } else if (kIntegrator == BH_INTEGRATOR_MULTI) {
-    h = trace_multi<R>(s, x, y, rk4_consts<R>(p), &steps);
+    h = trace_multi<R>(s, x, y, bulk_consts<R>(p), &steps);
   } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
     h = trace_ref<R, true>(s, x, y);
   } else if (s.n_objects > 0) {
-    h = trace_rk4_obj<R>(s, x, y, rk4_consts<R>(p), &steps);
+    h = trace_rk4_obj<R>(s, x, y, bulk_consts<R>(p), &steps);
   } else {
-    h = trace_rk4<R, false>(s, x, y, rk4_consts<R>(p), &steps);
+    h = trace_rk4<R, false>(s, x, y, bulk_consts<R>(p), &steps);
   }
   store_hit(s, p.format, x, y, h);
   if (p.counters) {
