@@ -10,9 +10,12 @@ output to compare with:
   direction, n = (1 + m/2rho)^3 / (1 - m/2rho); the bending is
   dphi - pi + chi + chi_e with chi_e the exit angle at the escape sphere.
   Bound 1e-8 rad at step 0.01 (fourth order: 3e-10 measured);
+- one hole: disc hits at the radius the inverted orbit integral gives at
+  the disc plane's crossing angles (isotropic radius within 1e-7 M);
 - one hole: rays with b below 3 sqrt(3) m are captured, above it escape;
 - an equal-mass binary seen from its mirror plane renders mirror
-  symmetric (classes exactly, the bending within 1e-9 rad).
+  symmetric (classes exactly, the bending within 1e-9 rad);
+- a third hole changes the image (every hole takes part).
 """
 import math
 
