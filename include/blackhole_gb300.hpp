@@ -19,11 +19,15 @@
 //   disc.SetTexture(blackhole::Texture::FromPixels(w, h, BH_TEXEL_BGR8, bytes));
 //   blackhole::Image screen = blackhole::Render(cam, bh, &disc, nullptr);   // BGR24, CV_8UC3 layout
 //
+// Rectangle<T>, Triangle<T>, InfinitePlane<T> and ChessPattern2D<T> are kept
+// as well: a Scene<T> lists them in `objects`.
+//
 // Additions the reference does not have: Annulus::r_inner()/r_outer()
 // (private there, vector_object.h:353-355), a Background (equirectangular
 // sky; the reference leaves missed rays black), Options (integrator,
-// precision, schedule ...), batched renders and the differentiable render's
-// adjoint. Everything goes through the C ABI of bh_gb300.h; failures throw
+// precision, schedule ...), batched renders, scenes with several holes
+// (Scene<T>::extra_holes with BH_INTEGRATOR_MULTI) and the differentiable
+// render's adjoint. Everything goes through the C ABI of bh_gb300.h; failures throw
 // blackhole::Error (where the reference calls std::terminate on an empty
 // texture, material.h:30-33, SetTexture throws).
 //
