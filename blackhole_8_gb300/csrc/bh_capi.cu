@@ -187,48 +187,8 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
 }
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
-  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4 &&
-      o.integrator != BH_INTEGRATOR_FLAT && o.integrator != BH_INTEGRATOR_MULTI)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
-  if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
-  if (o.integrator != BH_INTEGRATOR_RK4 && o.precision == BH_PRECISION_MIXED)
-    return set_err(ctx, BH_ERR_UNSUPPORTED, "MIXED precision applies to the RK4 integrator only");
-  if ((o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI) && o.schedule != BH_SCHEDULE_GRID)
-    return set_err(ctx, BH_ERR_UNSUPPORTED, "the FLAT and MULTI integrators run on the GRID schedule");
-  if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown raygen %d", o.raygen);
-  if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown format %d", o.format);
-  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "unknown schedule %d", o.schedule);
-  if (o.schedule == BH_SCHEDULE_PERSISTENT &&
-      (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
-    return set_err(ctx, BH_ERR_UNSUPPORTED, "the persistent schedule runs RK4 in FP32 or MIXED precision");
-  if (!(o.step > 0 && o.step <= 1.0)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "step must be in (0, 1]");
-  if (o.max_steps < 1 || o.max_steps > 100000000)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e8]");
-  if (!(o.r_escape > 2.0) || !std::isfinite(o.r_escape))
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "r_escape must exceed the horizon (2 M)");
-  if (!(o.band >= 0) || !std::isfinite(o.band)) return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band must be >= 0");
-  if (!(o.band_step > 0 && o.band_step <= 1.0))
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_step must be in (0, 1]");
-  if (!(o.setup_band >= 0) || !std::isfinite(o.setup_band))
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "setup_band must be >= 0");
-  if (o.slice_steps < 4 || o.slice_steps > 4096)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
-  if (o.band_lanes < 1 || o.band_lanes > 32)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_lanes must be in [1, 32]");
-  if (o.band_serial != 0 && o.band_serial != 1)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "band_serial must be 0 or 1");
-  if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
-  if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "threads_per_block must be a multiple of 32 in [32, 256]");
-  if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
-  if (o.refill_threshold < 1 || o.refill_threshold > 32)
-    return set_err(ctx, BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");
+  char msg[160];
+  if (int rc = bhgb::render_options_problem(o, msg, sizeof(msg))) return set_err(ctx, rc, "%s", msg);
   return BH_OK;
 }
 

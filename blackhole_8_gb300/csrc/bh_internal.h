@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 
 #include "bh_gb300.h"
@@ -301,6 +302,65 @@ inline void carve_band(uint32_t* base, uint32_t cap, uint32_t** list, uint32_t**
 inline float band_key_scale_for(double eps_lo, double eps_hi) {
   const double edge = std::fmax(std::fabs(eps_lo), std::fabs(eps_hi));
   return edge > 0 ? float(1.0 / edge) : 0.f;
+}
+
+// The checks of bh_render_options that need no context, shared by every
+// render entry point (bh_render, bh_render_device, bh_sequence_create,
+// bh_render_noalloc) so that they accept and refuse the same options.
+// Returns BH_OK, or a status with a message of at most `len` bytes in `msg`.
+inline int render_options_problem(const bh_render_options& o, char* msg, size_t len) {
+  auto bad = [&](int code, const char* text) {
+    std::snprintf(msg, len, "%s", text);
+    return code;
+  };
+  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4 &&
+      o.integrator != BH_INTEGRATOR_FLAT && o.integrator != BH_INTEGRATOR_MULTI) {
+    std::snprintf(msg, len, "unknown integrator %d", o.integrator);
+    return BH_ERR_INVALID_ARGUMENT;
+  }
+  if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED) {
+    std::snprintf(msg, len, "unknown precision %d", o.precision);
+    return BH_ERR_INVALID_ARGUMENT;
+  }
+  if (o.integrator != BH_INTEGRATOR_RK4 && o.precision == BH_PRECISION_MIXED)
+    return bad(BH_ERR_UNSUPPORTED, "MIXED precision applies to the RK4 integrator only");
+  if ((o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI) && o.schedule != BH_SCHEDULE_GRID)
+    return bad(BH_ERR_UNSUPPORTED, "the FLAT and MULTI integrators run on the GRID schedule");
+  if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE) {
+    std::snprintf(msg, len, "unknown raygen %d", o.raygen);
+    return BH_ERR_INVALID_ARGUMENT;
+  }
+  if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8) {
+    std::snprintf(msg, len, "unknown format %d", o.format);
+    return BH_ERR_INVALID_ARGUMENT;
+  }
+  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT) {
+    std::snprintf(msg, len, "unknown schedule %d", o.schedule);
+    return BH_ERR_INVALID_ARGUMENT;
+  }
+  if (o.schedule == BH_SCHEDULE_PERSISTENT && (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
+    return bad(BH_ERR_UNSUPPORTED, "the persistent schedule runs RK4 in FP32 or MIXED precision");
+  if (!(o.step > 0 && o.step <= 1.0)) return bad(BH_ERR_INVALID_ARGUMENT, "step must be in (0, 1]");
+  if (o.max_steps < 1 || o.max_steps > 100000000)
+    return bad(BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e8]");
+  if (!(o.r_escape > 2.0) || !std::isfinite(o.r_escape))
+    return bad(BH_ERR_INVALID_ARGUMENT, "r_escape must exceed the horizon (2 M)");
+  if (!(o.band >= 0) || !std::isfinite(o.band)) return bad(BH_ERR_INVALID_ARGUMENT, "band must be >= 0");
+  if (!(o.band_step > 0 && o.band_step <= 1.0)) return bad(BH_ERR_INVALID_ARGUMENT, "band_step must be in (0, 1]");
+  if (!(o.setup_band >= 0) || !std::isfinite(o.setup_band))
+    return bad(BH_ERR_INVALID_ARGUMENT, "setup_band must be >= 0");
+  if (o.slice_steps < 4 || o.slice_steps > 4096)
+    return bad(BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
+  if (o.band_lanes < 1 || o.band_lanes > 32) return bad(BH_ERR_INVALID_ARGUMENT, "band_lanes must be in [1, 32]");
+  if (o.band_serial != 0 && o.band_serial != 1) return bad(BH_ERR_INVALID_ARGUMENT, "band_serial must be 0 or 1");
+  if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
+    return bad(BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
+  if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
+    return bad(BH_ERR_INVALID_ARGUMENT, "threads_per_block must be a multiple of 32 in [32, 256]");
+  if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64) return bad(BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
+  if (o.refill_threshold < 1 || o.refill_threshold > 32)
+    return bad(BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");
+  return BH_OK;
 }
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.

@@ -13,14 +13,21 @@
 // fixed size. It calls no cudaMalloc, cudaFree, cudaMallocHost or other
 // allocating routine.
 //
-// The array (kScratchBytes, about 16 MiB) belongs to every device that loads
-// this library, for the life of the process. Its device address is taken
-// with cudaGetSymbolAddress the first time the entry point runs on a device
-// (with that device current); do that first call before any stream capture.
-// All calls share the array and it keeps the last call's contents: the
-// counters are cleared on the caller's stream at the start of each call, and
-// two calls whose work overlaps on the GPU (different streams, or the same
-// stream from different host threads without ordering) race on it.
+// The array (kScratchBytes, about 34 MiB: nearly all of it the band list,
+// 9 bytes per ray for BH_NOALLOC_MAX_RAYS rays) belongs to every device that
+// loads this library, for the life of the process. With lazy module loading
+// (the CUDA default) the device reserves it when the module is first loaded
+// on that device, which happens inside the first call of this entry point
+// there; that first call also takes the array's device address with
+// cudaGetSymbolAddress (with that device current) and keeps it for later
+// calls. Make that first call during set-up, before any stream capture. The
+// kept address is no longer valid after cudaDeviceReset on that device.
+// Each call stages its scene records from a static host array into the device
+// array with cudaMemcpyAsync. All calls share the array and it keeps the last
+// call's contents: the counters are cleared on the caller's stream at the
+// start of each call, and two calls whose work overlaps on the GPU
+// (different streams, or the same stream from different host threads
+// without ordering) race on it.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -44,6 +51,8 @@ constexpr size_t kCountersOffset = 0;
 constexpr size_t kScenesOffset = round_up(sizeof(DevCounters));
 constexpr size_t kBandOffset = kScenesOffset + round_up(sizeof(DevScene) * BH_NOALLOC_MAX_SCENES);
 constexpr size_t kScratchBytes = kBandOffset + sizeof(uint32_t) * bhgb::band_words(BH_NOALLOC_MAX_RAYS);
+// The size the header states ("about 34 MiB").
+static_assert(kScratchBytes > (33u << 20) && kScratchBytes < (35u << 20), "no-alloc scratch is about 34 MiB");
 
 // The scratch: counters | scene records | band list.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -155,26 +164,10 @@ int check(const bh_scene* scenes, int32_t n, const bh_device_texture* tex, int32
     return fail(err, len, BH_ERR_INVALID_ARGUMENT, "need 1..%d scenes with frames", BH_NOALLOC_MAX_SCENES);
   if (o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI)
     return fail(err, len, BH_ERR_UNSUPPORTED, "the no-alloc render has no FLAT or MULTI integrator");
-  if (o.integrator != BH_INTEGRATOR_REF_TRAPEZOID && o.integrator != BH_INTEGRATOR_RK4)
-    return fail(err, len, BH_ERR_INVALID_ARGUMENT, "unknown integrator %d", o.integrator);
-  if (o.precision < BH_PRECISION_FP32 || o.precision > BH_PRECISION_MIXED ||
-      (o.integrator == BH_INTEGRATOR_REF_TRAPEZOID && o.precision == BH_PRECISION_MIXED))
-    return fail(err, len, BH_ERR_UNSUPPORTED, "unsupported precision %d for this integrator", o.precision);
-  if (o.raygen != BH_RAYGEN_REF && o.raygen != BH_RAYGEN_PINHOLE)
-    return fail(err, len, BH_ERR_INVALID_ARGUMENT, "unknown raygen %d", o.raygen);
-  if (o.format < BH_FORMAT_BGRA8 || o.format > BH_FORMAT_RGBA8)
-    return fail(err, len, BH_ERR_INVALID_ARGUMENT, "unknown format %d", o.format);
-  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT)
-    return fail(err, len, BH_ERR_INVALID_ARGUMENT, "unknown schedule %d", o.schedule);
-  if (o.schedule == BH_SCHEDULE_PERSISTENT && (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
-    return fail(err, len, BH_ERR_UNSUPPORTED, "the persistent schedule runs RK4 in FP32 or MIXED precision");
-  if (!(o.step > 0 && o.step <= 1.0) || !(o.band_step > 0 && o.band_step <= 1.0) || o.max_steps < 1 ||
-      o.max_steps > 100000000 || !(o.r_escape > 2.0) || !std::isfinite(o.r_escape) || !(o.band >= 0) ||
-      !(o.setup_band >= 0) || o.slice_steps < 4 || o.slice_steps > 4096 || o.refill_threshold < 1 ||
-      o.refill_threshold > 32 || o.band_lanes < 1 || o.band_lanes > 32 || (o.band_serial != 0 && o.band_serial != 1) || o.block_x < 1 || o.block_y < 1 ||
-      o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0 || o.threads_per_block < 32 ||
-      o.threads_per_block > 256 || o.threads_per_block % 32 != 0 || o.blocks_per_sm < 0 || o.blocks_per_sm > 64)
-    return fail(err, len, BH_ERR_INVALID_ARGUMENT, "render options out of range");
+  {
+    char msg[160];
+    if (int rc = bhgb::render_options_problem(o, msg, sizeof(msg))) return fail(err, len, rc, "%s", msg);
+  }
   int64_t rays = 0;
   for (int i = 0; i < n; ++i) {
     const bh_scene& s = scenes[i];

@@ -353,9 +353,13 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
  * in one fixed device array of about 34 MiB that every device loading the
  * library holds until exit; calls are limited to BH_NOALLOC_MAX_SCENES scenes
  * and BH_NOALLOC_MAX_RAYS rays (scenes padded to 8x4 tiles) and are rejected
- * with BH_ERR_INVALID_ARGUMENT above that. The first call on a device takes
- * the array's address (make it before any stream capture). All calls share
- * the array: calls whose work overlaps on the GPU race. Enqueued on `stream`
+ * with BH_ERR_INVALID_ARGUMENT above that. The first call on a device loads
+ * the library's device code there, which reserves the array, and takes the
+ * array's address: make that first call during set-up, before any stream
+ * capture. The address is kept for later calls and is no longer valid after
+ * cudaDeviceReset. Each call copies its scene records from a static host
+ * array with cudaMemcpyAsync. All calls share the array: calls whose work
+ * overlaps on the GPU race. Enqueued on `stream`
  * (a cudaStream_t, NULL = the legacy default stream); returns without
  * waiting. `error` (may be NULL) receives a message of at most error_len
  * bytes. */

@@ -34,7 +34,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 SRC_DIR = os.path.join(REF_DIR, "src")
 RUNNER = os.path.join(REF_DIR, "ref_runner")
-REFERENCE_ROOT = os.environ.get("BH_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $BH_REFERENCE_ROOT, else a sibling directory
+# named "reference" next to this repository.
+REFERENCE_ROOT = os.environ.get("BH_REFERENCE_ROOT",
+                                os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 
 LOOP_FILE = "include/blackhole/blackhole_solution_test.cc"
 LOOP_FIRST, LOOP_SPLIT, LOOP_LAST = 161, 162, 308
