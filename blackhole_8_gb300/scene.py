@@ -473,8 +473,10 @@ def value_noise_background(seed: int, width: int = 2048, height: int = 1024, oct
             ty = ty * ty * (3 - 2 * ty)
             ix0, ix1 = ix % cx, (ix + 1) % cx
             iy0, iy1 = np.minimum(iy, cy), np.minimum(iy + 1, cy)
+            # lattice values, hashed once per lattice point
+            lattice = hash_u01(seed, 10 + ch, o, np.arange(cy + 1)[:, None], np.arange(cx)[None, :])
             def lat(a, b):
-                return hash_u01(seed, 10 + ch, o, b[:, None], a[None, :])
+                return lattice[b[:, None], a[None, :]]
             v00, v10 = lat(ix0, iy0), lat(ix1, iy0)
             v01, v11 = lat(ix0, iy1), lat(ix1, iy1)
             top = v00 + (v10 - v00) * tx[None, :]
@@ -681,3 +683,54 @@ def photon_ring_scene(side: int = 4096, fov_deg: float = 0.5, radius: float = 20
     cam.RotateZ(math.asin(b_c / radius))
     return Scene(cam, StaticBlackhole((0.0, 0.0, 0.0), 1.0), equatorial_disc(6.0, 20.0, disc_tex), bg,
                  {"workload": f"photon ring {side}x{side}"})
+
+
+def ref_impact_parameter(scene: Scene, xs, ys) -> np.ndarray:
+    """b / M of the ray of pixels (xs, ys) under REF ray generation: the
+    reference forms the ray direction e = F - pv from the camera focus F and
+    the point pv = PixelVector(x, y) - hole (blackhole_solution_test.cc:
+    167-170), and the orbit's impact parameter is b = |F x e| / |e| with F
+    relative to the hole. Vectorised over the pixels, FP64."""
+    cam, hole = scene.camera, scene.hole
+    a = cam.width() / 2.0 - np.asarray(xs, dtype=np.float64)
+    c = cam.height() / 2.0 - np.asarray(ys, dtype=np.float64)
+    F = cam.position() - hole.center()
+    E0 = cam.position() - cam.focus_vector()
+    e = E0[None, :] + a.reshape(-1, 1) * cam.vector_y()[None, :] + c.reshape(-1, 1) * cam.vector_z()[None, :]
+    fe = np.cross(F[None, :], e)
+    b = np.sqrt((fe * fe).sum(1) / (e * e).sum(1)) / hole.mass()
+    return b.reshape(np.shape(xs))
+
+
+def impact_grid_scene(side: int = 4096, window: float = 1e-4, radius: float = 20.0, seed: int = 0) -> Scene:
+    """Near-critical stress set: a side x side image whose rays have impact
+    parameters spread uniformly over 3 sqrt(3) M +- window M, every pixel a
+    different value. The camera at `radius` has a field of view of ~1e-5 rad
+    aimed at the photon ring, so b changes linearly along the image rows; it
+    is turned about its view axis by atan(1 / side) so that the rows also
+    step b by 1/side of a column: b follows the pixel's raster index
+    x * side + y. Same hole, disc and sky as the single scene."""
+    b_c = 3.0 * math.sqrt(3.0)
+    base = photon_ring_scene(side, 0.5, radius, seed)
+    cam = base.camera
+    mid = side / 2.0
+    ends = np.array([0.0, side - 1.0])
+
+    def b_at(xs, ys):
+        return ref_impact_parameter(base, np.asarray(xs, dtype=np.float64), np.asarray(ys, dtype=np.float64))
+
+    # narrow the field of view until a row spans 2 window (b is linear in the
+    # column to ~1e-9 at these angles), then aim the centre at b_c
+    for _ in range(3):
+        lo, hi = b_at(ends, [mid, mid])
+        want = 2.0 * window * (side - 1.0) / side
+        cam.fov(2.0 * math.atan(math.tan(cam.fov() / 2.0) * want / abs(hi - lo)))
+    for _ in range(4):
+        bc0 = float(b_at([mid], [mid])[0])
+        d = 1e-9
+        cam.RotateZ(d)
+        bc1 = float(b_at([mid], [mid])[0])
+        cam.RotateZ((b_c - bc1) * d / (bc1 - bc0))
+    cam.RotateX(math.atan(1.0 / side))
+    base.meta = {"workload": f"impact-parameter grid {side}x{side}, b = 3 sqrt(3) M +- {window:g} M"}
+    return base

@@ -204,6 +204,7 @@ static vec3 pixel_vector(const view* v, int x, int y, vec3 fv) {
 
 static double frac_margin(double f) {
   double d = f - floor(f);
+  if (d != d) return 0.0; /* NaN coordinates: no margin */
   return d < 0.5 ? d : 1.0 - d;
 }
 
@@ -373,24 +374,44 @@ static int collide_object(const bh_object* o, vec3 p1, vec3 p2, vec3* hit) {
 }
 
 /* ChessPattern2D<T>{size}, pattern.h:23-46 ((int) casts pinned) */
-static void chess(double size, double x, double y, uint8_t out[4]) {
+static double chess_axis_margin(double size, int m, double b, double c2) {
+  /* the colour changes where c2 crosses 0 or size (c2 in [0, 2 size)), where
+   * trunc(|c|) crosses a multiple of m (the cell index) and where c changes
+   * sign; the distance to the nearest of these, in units of size */
+  double d = fabs(c2);
+  if (fabs(c2 - size) < d) d = fabs(c2 - size);
+  if (fabs(2 * size - c2) < d) d = fabs(2 * size - c2);
+  double k = b / m;
+  double dk = fabs(b - floor(k + 0.5) * m);
+  if (dk < d) d = dk;
+  if (b < d) d = b;
+  return d == d ? d / size : 0.0; /* NaN coordinates: no margin */
+}
+
+static void chess(double size, double x, double y, uint8_t out[4], double* margin) {
   int m = trunc_int(size * 2);
   int white = 0;
+  if (margin) *margin = 1.0;
   if (m != 0) {
     double bx = fabs(x), by = fabs(y);
     double x2 = bx - (double)(trunc_int(bx) / m) * (size * 2);
     double y2 = by - (double)(trunc_int(by) / m) * (size * 2);
     int in = (x2 <= size && y2 <= size) || (size <= x2 && size <= y2);
     white = x * y > 0 ? in : !in;
+    if (margin) {
+      double a = chess_axis_margin(size, m, bx, x2), b = chess_axis_margin(size, m, by, y2);
+      *margin = a < b ? a : b;
+    }
   }
   out[0] = out[1] = out[2] = white ? 255 : 0;
 }
 
 /* Rectangle::color (vector_object.h:163-180), InfinitePlane::color (:227-232),
  * Material::color for triangles (black) */
-static void color_object(const view* v, int i, vec3 p, uint8_t out[4]) {
+static void color_object(const view* v, int i, vec3 p, uint8_t out[4], double* margin) {
   const bh_object* o = &v->obj[i];
   out[0] = out[1] = out[2] = 0;
+  if (margin) *margin = 1.0;
   if (o->type == BH_OBJECT_RECTANGLE) {
     const orc_texture* t = v->obj_tex ? &v->obj_tex[i] : NULL;
     if (!t || !t->bgra) return;
@@ -400,15 +421,20 @@ static void color_object(const view* v, int i, vec3 p, uint8_t out[4]) {
     double r = sqrt(dot(q, q));
     double theta = acos(dot(s1, q) / (sqrt(dot(s1, s1)) * r));
     theta = isnan(theta) ? 0 : theta;
-    int px_w = trunc_int((r * cos(theta) / sqrt(dot(s1, s1))) * t->width);
-    int px_h = trunc_int((r * sin(theta) / sqrt(dot(s2, s2))) * t->height);
+    double fw = (r * cos(theta) / sqrt(dot(s1, s1))) * t->width;
+    double fh = (r * sin(theta) / sqrt(dot(s2, s2))) * t->height;
+    int px_w = trunc_int(fw), px_h = trunc_int(fh);
     read_texel(t, (long long)px_h * t->width + px_w, out);
+    if (margin) {
+      double a = frac_margin(fw), b = frac_margin(fh);
+      *margin = a < b ? a : b;
+    }
   } else if (o->type == BH_OBJECT_PLANE && o->pattern_size > 0) {
     const double* vx = o->axis_x;
     const double* vy = o->axis_y;
     double b = (vx[0] * p.y - vx[1] * p.x) / (vx[0] * vy[1] - vx[1] * vy[0]);
     double a = (p.x - b * vy[0]) / vx[0];
-    chess(o->pattern_size, a, b, out);
+    chess(o->pattern_size, a, b, out, margin);
   }
 }
 
@@ -436,7 +462,9 @@ static int nearest_object(const view* v, vec3 p1, vec3 p2, double* dd_out, vec3*
 /* ObjectManager::FindCollision: nearest to p1 over the objects, the hole
  * (with_hole) and the disc; returns the class, writes the colour and, for an
  * object, its index. */
-static int find_collision_objects(const view* v, vec3 p1, vec3 p2, int with_hole, uint8_t out[4], int* obj_out) {
+/* margin (may be NULL): the colour's distance to a texel or pattern edge. */
+static int find_collision_objects(const view* v, vec3 p1, vec3 p2, int with_hole, uint8_t out[4], int* obj_out,
+                                  double* margin) {
   int cls = BH_CLASS_MISS, obj = -1;
   double best = 0;
   vec3 hp = v3(0, 0, 0), h;
@@ -461,14 +489,14 @@ static int find_collision_objects(const view* v, vec3 p1, vec3 p2, int with_hole
     }
   }
   out[0] = out[1] = out[2] = 0;
-  if (cls == BH_CLASS_DISC) color_disc(v, hp, out, NULL);
-  if (cls == BH_CLASS_OBJECT) color_object(v, obj, hp, out);
+  if (cls == BH_CLASS_DISC) color_disc(v, hp, out, margin);
+  if (cls == BH_CLASS_OBJECT) color_object(v, obj, hp, out, margin);
   if (obj_out) *obj_out = cls == BH_CLASS_OBJECT ? obj : -1;
   return cls;
 }
 
-static int find_collision(const view* v, vec3 p1, vec3 p2, uint8_t out[4]) {
-  return find_collision_objects(v, p1, p2, 1, out, NULL);
+static int find_collision(const view* v, vec3 p1, vec3 p2, uint8_t out[4], double* margin) {
+  return find_collision_objects(v, p1, p2, 1, out, NULL, margin);
 }
 
 /* StaticBlackhole::G, InvSqrtG, SolveG (blackhole_solution.h:27-53) */
@@ -511,7 +539,7 @@ static vec3 back_project(const view* v, const plane* p, double r, double phi) {
 }
 
 /* ------------------------------------------------------------------------- */
-static int ref_pixel(const view* v, int x, int y, uint8_t out[4]) {
+static int ref_pixel(const view* v, int x, int y, uint8_t out[4], double* margin) {
   plane p;
   reduce(v, x, y, &p);
   const double b = p.Fc.z;
@@ -533,7 +561,7 @@ static int ref_pixel(const view* v, int x, int y, uint8_t out[4]) {
     phi += (dphi_prev + dphi) * du_h;
     cur = back_project(v, &p, 1. / u, phi);
     dphi_prev = dphi;
-    if ((cls = find_collision(v, prev, cur, out)) != BH_CLASS_MISS) return cls;
+    if ((cls = find_collision(v, prev, cur, out, margin)) != BH_CLASS_MISS) return cls;
     prev = cur;
   }
   u += du * 0.9;
@@ -541,15 +569,15 @@ static int ref_pixel(const view* v, int x, int y, uint8_t out[4]) {
   phi += (dphi_prev + dphi) * du_h;
   cur = back_project(v, &p, 1. / u, phi);
   dphi_prev = dphi;
-  if ((cls = find_collision(v, prev, cur, out)) != BH_CLASS_MISS) return cls;
+  if ((cls = find_collision(v, prev, cur, out, margin)) != BH_CLASS_MISS) return cls;
   prev = cur;
-  if (sol < 0) return find_collision(v, prev, v->hole, out);
+  if (sol < 0) return find_collision(v, prev, v->hole, out, margin);
   for (int i = 0; i < nstep_safe; ++i) {
     u -= du;
     dphi = inv_sqrt_G(v->M, u, b);
     phi += (dphi_prev + dphi) * du_h;
     cur = back_project(v, &p, 1. / u, phi);
-    if ((cls = find_collision(v, prev, cur, out)) != BH_CLASS_MISS) return cls;
+    if ((cls = find_collision(v, prev, cur, out, margin)) != BH_CLASS_MISS) return cls;
     dphi_prev = dphi;
     prev = cur;
   }
@@ -742,7 +770,7 @@ static void rk4_pixel_obj(const view* v, const orc_rk4_opts* o, int x, int y, rk
     if (f_obj <= 1) {
       res->cls = BH_CLASS_OBJECT;
       res->aux = obj;
-      color_object(v, obj, ohit, res->bgra);
+      color_object(v, obj, ohit, res->bgra, &res->margin_tex);
       res->steps = k + 1;
       return;
     }
@@ -779,7 +807,7 @@ static void rk4_pixel_obj(const view* v, const orc_rk4_opts* o, int x, int y, rk
 }
 
 /* The flat RayTracer (REF ray generation): ten chords, then a miss. */
-static int flat_pixel(const view* v, int x, int y, uint8_t out[4], int* obj) {
+static int flat_pixel(const view* v, int x, int y, uint8_t out[4], int* obj, double* margin) {
   vec3 fv = scale(v->vx, v->focus_len);
   vec3 old = v->focus;
   vec3 pres = pixel_vector(v, x, y, fv);
@@ -787,7 +815,7 @@ static int flat_pixel(const view* v, int x, int y, uint8_t out[4], int* obj) {
   double d2 = dot(vec, vec);
   if (d2 < 100) vec = scale(vec, 100.0 / d2);
   for (int i = 0; i < 10; ++i) {
-    int cls = find_collision_objects(v, old, pres, 0, out, obj);
+    int cls = find_collision_objects(v, old, pres, 0, out, obj, margin);
     if (cls != BH_CLASS_MISS) return cls;
     vec3 next = add(pres, vec);
     old = pres;
@@ -926,7 +954,7 @@ static void multi_pixel(const view* v, const orc_rk4_opts* o, int x, int y, rk4_
     if (f_obj <= 1) {
       res->cls = BH_CLASS_OBJECT;
       res->aux = obj;
-      color_object(v, obj, ohit, res->bgra);
+      color_object(v, obj, ohit, res->bgra, &res->margin_tex);
       ++k;
       break;
     }
@@ -981,10 +1009,12 @@ int orc_render_ref(const bh_scene* s, const orc_texture* disc_tex, const orc_tex
     int x = pixels ? pixels[2 * i] : (int)(i % v.W);
     int y = pixels ? pixels[2 * i + 1] : (int)(i / v.W);
     uint8_t c[4] = {0, 0, 0, 255};
-    int cls = ref_pixel(&v, x, y, c);
+    double mt = 1.0;
+    int cls = ref_pixel(&v, x, y, c, &mt);
     c[3] = 255;
     if (out->bgra) memcpy(out->bgra + 4 * i, c, 4);
     if (out->cls) out->cls[i] = (uint8_t)cls;
+    if (out->margin_tex) out->margin_tex[i] = cls == BH_CLASS_DISC || cls == BH_CLASS_OBJECT ? mt : 1.0;
   }
   return 0;
 }
@@ -1030,11 +1060,13 @@ int orc_render_flat(const bh_scene* s, const orc_texture* disc_tex, const orc_te
     int y = pixels ? pixels[2 * i + 1] : (int)(i / v.W);
     uint8_t c[4] = {0, 0, 0, 255};
     int obj = -1;
-    int cls = flat_pixel(&v, x, y, c, &obj);
+    double mt = 1.0;
+    int cls = flat_pixel(&v, x, y, c, &obj, &mt);
     c[3] = 255;
     if (out->bgra) memcpy(out->bgra + 4 * i, c, 4);
     if (out->cls) out->cls[i] = (uint8_t)cls;
     if (out->aux) out->aux[i] = obj;
+    if (out->margin_tex) out->margin_tex[i] = cls == BH_CLASS_DISC || cls == BH_CLASS_OBJECT ? mt : 1.0;
   }
   return 0;
 }

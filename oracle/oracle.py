@@ -120,7 +120,10 @@ def _pixels(pixels):
 
 
 def render_ref(scene, pixels=None, threads: int = 0) -> dict:
-    """Oracle A: the reference's trapezoid render, FP64."""
+    """Oracle A: the reference's trapezoid render, FP64. margin_tex: for disc
+    and object hits, the distance (texels, or pattern cells for the chess
+    plane) of the colour's sampling coordinate to the nearest edge where the
+    colour can change; 1 elsewhere."""
     lib = load()
     s = _scene_c(scene)
     dt, dta = _tex(scene.disc.texture if scene.disc is not None else None)
@@ -129,10 +132,11 @@ def render_ref(scene, pixels=None, threads: int = 0) -> dict:
         n = scene.camera.width() * scene.camera.height()
     bgra = np.zeros((n, 4), np.uint8)
     cls = np.zeros(n, np.uint8)
-    out = OrcOutputs(bgra.ctypes.data, cls.ctypes.data, None, None, None, None, None)
+    margin = np.zeros(n)
+    out = OrcOutputs(bgra.ctypes.data, cls.ctypes.data, None, margin.ctypes.data, None, None, None)
     ot, otk = _obj_tex(scene)
     lib.orc_render_ref(C.byref(s), C.byref(dt) if dt else None, ot, pp, n, C.byref(out), threads)
-    res = {"bgra": bgra, "cls": cls}
+    res = {"bgra": bgra, "cls": cls, "margin_tex": margin}
     if pixels is None:
         h, w = scene.camera.height(), scene.camera.width()
         res = {k: v.reshape((h, w) + v.shape[1:]) for k, v in res.items()}
@@ -184,8 +188,10 @@ def render_flat(scene, pixels=None, threads: int = 0) -> dict:
     pp, n, keep = _pixels(pixels)
     if pp is None:
         n = scene.camera.width() * scene.camera.height()
-    res = {"bgra": np.zeros((n, 4), np.uint8), "cls": np.zeros(n, np.uint8), "aux": np.zeros(n)}
-    out = OrcOutputs(res["bgra"].ctypes.data, res["cls"].ctypes.data, res["aux"].ctypes.data, None, None, None, None)
+    res = {"bgra": np.zeros((n, 4), np.uint8), "cls": np.zeros(n, np.uint8), "aux": np.zeros(n),
+           "margin_tex": np.zeros(n)}
+    out = OrcOutputs(res["bgra"].ctypes.data, res["cls"].ctypes.data, res["aux"].ctypes.data,
+                     res["margin_tex"].ctypes.data, None, None, None)
     lib.orc_render_flat(C.byref(s), C.byref(dt) if dt else None, ot, pp, n, C.byref(out), threads)
     if pixels is None:
         h, w = scene.camera.height(), scene.camera.width()

@@ -90,6 +90,18 @@ def build(name: str, width: int, height: int) -> S.Scene:
     return BUILDERS[name](width, height)
 
 
+# Colours may differ where the sampling coordinate lies within this many
+# texels (or chess cells) of an edge: there FP64 rounding of the hit point
+# alone decides which texel is read (a tie). The reference's own output and
+# the FP64 restatement differ only at margins of ~1e-14 texels.
+TEXEL_TIE_FP64 = 1e-6
+
+
+def colour_lsb(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Largest per-channel difference of two BGR(A) images, in 8-bit LSB."""
+    return np.abs(a[..., :3].astype(np.int16) - b[..., :3].astype(np.int16)).max(-1)
+
+
 def class_boundary_mask(cls: np.ndarray) -> np.ndarray:
     """Pixels with a 4-neighbour of another class."""
     m = np.zeros(cls.shape, dtype=bool)

@@ -20,6 +20,7 @@ import numpy as np
 import pytest
 
 import helpers
+from parity import boundary_pixels, compare, dilate, sample_check
 from blackhole_8_gb300 import capi
 from blackhole_8_gb300 import scene as S
 from oracle import oracle
@@ -35,40 +36,41 @@ def opts(**kw):
     return capi.default_options(**kw)
 
 
-def dilate(mask, n=1):
-    m = mask.copy()
-    for _ in range(n):
-        m2 = m.copy()
-        m2[1:, :] |= m[:-1, :]
-        m2[:-1, :] |= m[1:, :]
-        m2[:, 1:] |= m[:, :-1]
-        m2[:, :-1] |= m[:, 1:]
-        m = m2
-    return m
-
-
 # ---------------------------------------------------------------------------
 # the reference's trapezoid scheme
 @pytest.mark.parametrize("case", CASES, ids=lambda c: c["file"])
 def test_trapezoid_fp64_matches_reference(renderer, case):
     """The reference's curved loop (or, for flat cases, its RayTracer) in
-    FP64 on the GPU against the reference's own output."""
+    FP64 on the GPU against the reference's own output: hit classes agree on
+    >= 99.9 % of pixels and differ only on class boundaries; where the
+    classes agree, colours are within 1 LSB except where the oracle's
+    sampling coordinate lies within 1e-6 texels of a texel edge (a tie that
+    FP64 rounding of the hit point decides)."""
     sc = helpers.build(case["builder"], case["width"], case["height"])
     g = np.load(os.path.join(GOLDEN, case["file"]))
     flat = case.get("mode") == "flat"
     integ = capi.INTEGRATOR_FLAT if flat else capi.INTEGRATOR_REF_TRAPEZOID
     o = opts(integrator=integ, precision=capi.PRECISION_FP64, format=capi.FORMAT_BGR8)
     out = renderer.render([sc], o, hit_class=True, aux=flat)[0]
+    margin = (oracle.render_flat(sc) if flat else oracle.render_ref(sc))["margin_tex"]
+    boundary = dilate(helpers.class_boundary_mask(g["cls"]))
     if flat:
         idx = np.where(out.hit_class == capi.CLASS_OBJECT, out.aux, -1).astype(np.int32)
-        assert (idx != g["obj"]).mean() <= 1e-3
+        assert (idx != g["obj"]).mean() <= 1e-3 and not ((idx != g["obj"]) & ~boundary).any()
     bad = out.hit_class != g["cls"]
-    assert bad.mean() <= 1e-3 and not (bad & ~dilate(helpers.class_boundary_mask(g["cls"]))).any()
-    diff = (out.pixels != g["bgr"]).any(-1)
-    assert diff.mean() <= 2e-3, f"{diff.sum()} pixels differ"
+    assert bad.mean() <= 1e-3 and not (bad & ~boundary).any()
+    tie = margin < helpers.TEXEL_TIE_FP64
+    dl = helpers.colour_lsb(out.pixels, g["bgr"])
+    strict = ~bad & ~tie
+    assert dl[strict].max(initial=0) <= 1, f"{(dl[strict] > 1).sum()} pixels differ away from texel edges"
 
 
 def test_trapezoid_fp32_matches_oracle(renderer):
+    """The reference's scheme in FP32 against the FP64 oracle: classes agree
+    on >= 99.5 % of pixels, the rest within two pixels of a class boundary;
+    colours within 1 LSB where the classes agree and the sampling coordinate
+    lies 1e-3 texels or more from a texel edge (FP32 rounding of the hit
+    point is ~1e-4 texels)."""
     sc = helpers.cfg0_planar(160, 90)
     ref = oracle.render_ref(sc)
     o = opts(integrator=capi.INTEGRATOR_REF_TRAPEZOID, precision=capi.PRECISION_FP32)
@@ -76,6 +78,8 @@ def test_trapezoid_fp32_matches_oracle(renderer):
     bad = out.hit_class != ref["cls"]
     assert bad.mean() <= 5e-3
     assert not (bad & ~dilate(helpers.class_boundary_mask(ref["cls"]), 2)).any()
+    strict = ~bad & (ref["margin_tex"] >= 1e-3) & ~dilate(helpers.class_boundary_mask(ref["cls"]), 2)
+    assert helpers.colour_lsb(out.pixels, ref["bgra"])[strict].max(initial=0) <= 1
 
 
 # ---------------------------------------------------------------------------
@@ -84,33 +88,6 @@ def test_trapezoid_fp32_matches_oracle(renderer):
 def single():
     sc = S.single_scene(320, 180)
     return sc, oracle.render_rk4(sc)
-
-
-def boundary_pixels(o, band=0.05, tex=0.02, edge=2e-3):
-    """Pixels whose result may flip under rounding: next to another class,
-    near a disc edge, near the critical impact parameter or near a texel
-    edge."""
-    m = dilate(helpers.class_boundary_mask(o["cls"]))
-    m |= (o["cls"] == capi.CLASS_DISC) & (o["margin_r"] < edge)
-    m |= np.abs(o["b_over_m"] - B_C) < band
-    m |= o["margin_tex"] < tex
-    return m
-
-
-def compare(out, o, boundary, aux_tol, colour_lsb=1):
-    cls_ok = out.hit_class == o["cls"]
-    assert cls_ok.mean() >= 0.999, f"class agreement {cls_ok.mean():.5f}"
-    assert not (~cls_ok & ~boundary).any(), "class mismatch away from boundaries"
-    strict = cls_ok & ~boundary
-    dcol = np.abs(out.pixels[..., :3].astype(int) - o["bgra"][..., :3].astype(int)).max(-1)
-    assert dcol[strict].max(initial=0) <= colour_lsb
-    esc = strict & (o["cls"] == capi.CLASS_MISS)
-    dsk = strict & (o["cls"] == capi.CLASS_DISC)
-    err_esc = np.abs(out.aux[esc] - o["aux"][esc]).max(initial=0)
-    err_dsk = np.abs(out.aux[dsk] - o["aux"][dsk]).max(initial=0)
-    assert err_esc <= aux_tol, f"deflection error {err_esc}"
-    assert err_dsk <= max(aux_tol, 1e-3), f"hit radius error {err_dsk}"
-    return err_esc, err_dsk
 
 
 def test_rk4_fp64_matches_oracle(renderer, single):
@@ -180,39 +157,72 @@ def test_pinhole_raygen_differs_from_ref(renderer):
     assert (a != b).any()
 
 
-def test_full_hd_frames_sampled_against_oracle(renderer):
-    """Full-size 1920x1080 fly-through frames; a seeded pixel sample of each is
-    checked against the FP64 oracle."""
+@pytest.mark.parametrize("precision,schedule", [(capi.PRECISION_FP64, capi.SCHEDULE_GRID),
+                                                (capi.PRECISION_FP32, capi.SCHEDULE_GRID),
+                                                (capi.PRECISION_MIXED, capi.SCHEDULE_GRID),
+                                                (capi.PRECISION_MIXED, capi.SCHEDULE_PERSISTENT)],
+                         ids=["fp64", "fp32", "mixed-grid", "mixed-persistent"])
+def test_cfg0_full_size(renderer, precision, schedule):
+    """The single-scene workload at its own 640x360 against the FP64 oracle,
+    every pixel: FP64 to rounding, MIXED within 1e-4 rad on every escaped
+    ray, plain FP32 within 1e-4 rad outside |b - b_c| < 0.1 M."""
+    sc = S.single_scene(640, 360)
+    o = oracle.render_rk4(sc)
+    out = renderer.render([sc], opts(precision=precision, schedule=schedule), hit_class=True, aux=True)[0]
+    if precision == capi.PRECISION_FP64:
+        compare(out, o, boundary_pixels(o, band=1e-6, tex=1e-6, edge=1e-9), aux_tol=1e-6)
+    elif precision == capi.PRECISION_FP32:
+        compare(out, o, boundary_pixels(o, band=0.1), aux_tol=1e-4)
+    else:
+        compare(out, o, boundary_pixels(o, band=1e-4), aux_tol=1e-4)
+
+
+@pytest.mark.parametrize("step", [0.01, 0.1])
+def test_full_hd_frames_sampled_against_oracle(renderer, step):
+    """Full-size 1920x1080 fly-through frames through the mixed tracer on the
+    persistent schedule, at the oracle's step and at the step the autotuner
+    picks for the fly-through; 4000 seeded pixels of each frame against the
+    FP64 oracle (step 0.01) with the full parity bar (hit radius within
+    2e-3 M at step 0.1)."""
     scenes = S.flythrough(120)
-    picks = [scenes[0], scenes[60], scenes[119]]
-    out = renderer.render(picks, opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT),
+    picks = [scenes[0], scenes[39], scenes[79], scenes[119]]
+    out = renderer.render(picks, opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, step=step),
                           hit_class=True, aux=True)
     rng = np.random.default_rng(11)
     for sc, fb in zip(picks, out):
-        xs = rng.integers(0, 1920, 3000)
-        ys = rng.integers(0, 1080, 3000)
+        xs = rng.integers(0, 1920, 4000)
+        ys = rng.integers(0, 1080, 4000)
         o = oracle.render_rk4(sc, pixels=np.stack([xs, ys], 1))
-        cls = fb.hit_class[ys, xs]
-        agree = cls == o["cls"]
-        assert agree.mean() >= 0.998
-        esc = agree & (o["cls"] == capi.CLASS_MISS)
-        dsk = agree & (o["cls"] == capi.CLASS_DISC)
-        assert np.abs(fb.aux[ys, xs][esc] - o["aux"][esc]).max(initial=0) <= 1e-4
-        assert np.abs(fb.aux[ys, xs][dsk] - o["aux"][dsk]).max(initial=0) <= 2e-3
+        sample_check(sc, xs, ys, fb.hit_class[ys, xs], fb.pixels[ys, xs], fb.aux[ys, xs], o, {},
+                     radius_tol=1e-3 if step <= 0.01 else 2e-3)
 
 
 def test_batched_uneven_scenes(renderer):
-    scenes = S.batched_scenes(12, seed=3, min_side=32, max_side=160, bg_size=(256, 128))
+    """Uneven scenes (sides 32-160, each its own M, camera, disc and sky) in
+    one persistent mixed-precision launch: every scene against the FP64
+    oracle, every pixel, with the full parity bar over the batch (class
+    agreement counted over all its pixels)."""
+    scenes = S.batched_scenes(24, seed=3, min_side=32, max_side=160, bg_size=(256, 128))
     out = renderer.render(scenes, opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT),
                           hit_class=True, aux=True)
     st = renderer.stats()
     assert st.rays == sum(s.camera.width() * s.camera.height() for s in scenes)
+    agree = total = 0
     for sc, fb in zip(scenes, out):
         o = oracle.render_rk4(sc)
-        agree = fb.hit_class == o["cls"]
-        assert agree.mean() >= 0.995, sc.meta
-        esc = agree & (o["cls"] == capi.CLASS_MISS)
-        assert np.abs(fb.aux[esc] - o["aux"][esc]).max(initial=0) <= 1e-4
+        cls_ok = fb.hit_class == o["cls"]
+        agree += int(cls_ok.sum())
+        total += cls_ok.size
+        bnd = boundary_pixels(o, band=1e-4)
+        assert not (~cls_ok & ~bnd).any(), sc.meta
+        strict = cls_ok & ~bnd
+        assert helpers.colour_lsb(fb.pixels, o["bgra"])[strict].max(initial=0) <= 1, sc.meta
+        esc = strict & (o["cls"] == capi.CLASS_MISS)
+        dsk = strict & (o["cls"] == capi.CLASS_DISC)
+        assert np.abs(fb.aux[esc] - o["aux"][esc]).max(initial=0) <= 1e-4, sc.meta
+        # the hit radius, in units of the scene's M
+        assert np.abs(fb.aux[dsk] - o["aux"][dsk]).max(initial=0) <= 1e-3, sc.meta
+    assert agree / total >= 0.999
 
 
 @pytest.mark.parametrize("band", [5e-4, 0.05, 0.2])

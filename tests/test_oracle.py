@@ -36,9 +36,11 @@ def test_oracle_a_matches_reference_fixture(case):
     else:
         o = oracle.render_ref(sc)
     assert np.array_equal(o["cls"], g["cls"]), "hit classes differ from the reference"
-    diff = (o["bgra"][..., :3] != g["bgr"]).any(-1)
-    # colour differences only where a texel-edge tie rounds the other way
-    assert diff.mean() <= 2e-3, f"{diff.sum()} pixels differ in colour"
+    # colours equal except where a texel-edge tie rounds the other way
+    tie = o["margin_tex"] < helpers.TEXEL_TIE_FP64
+    dl = helpers.colour_lsb(o["bgra"], g["bgr"])
+    assert dl[~tie].max(initial=0) == 0, f"{(dl[~tie] > 0).sum()} pixels differ away from texel edges"
+    assert tie.mean() <= 2e-2
 
 
 def test_oracle_a_matches_live_reference():
@@ -50,7 +52,8 @@ def test_oracle_a_matches_live_reference():
     img, cls = refbridge.render_with_classes(sc)
     o = oracle.render_ref(sc)
     assert np.array_equal(o["cls"], cls)
-    assert (o["bgra"][..., :3] != img).any(-1).mean() <= 2e-3
+    tie = o["margin_tex"] < helpers.TEXEL_TIE_FP64
+    assert helpers.colour_lsb(o["bgra"], img)[~tie].max(initial=0) == 0
 
 
 def test_fixture_classes_are_nontrivial():
