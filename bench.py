@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-objects", action="store_true", help="skip the objects / flat tracer leg")
+    ap.add_argument("--no-stress", action="store_true",
+                    help="skip the near-critical (photon ring, impact grid) and 256-scene batch legs")
     return ap.parse_args()
 
 
@@ -194,13 +196,17 @@ ADJ_WORKLOAD = "adjoint 512x512: MSE vs target at M+5%, disc tilt +3 deg, r_out 
                "gradient w.r.t. M, camera position and yaw/pitch/roll, disc tilt, r_in, r_out; checkpoints every 64 steps"
 
 
-def time_sequence(r, args, scenes, opts):
-    """Mean device time of K replays (after W) of the scenes captured as one
-    sequence (CUDA graph), CUDA events on the context's stream."""
+def time_sequence(r, args, scenes, opts, steps=None, warmup=None, flush=None):
+    """Mean device time of `steps` replays (after `warmup`; default the
+    run's K and W) of the scenes captured as one sequence (CUDA graph), CUDA
+    events on the context's stream; with `flush` (a tensor larger than L2)
+    L2 is flushed before each timed replay, outside its events."""
     import torch
 
     from blackhole_8_gb300 import capi
 
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     cs = r.c_scenes(scenes)
     bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
             for s in scenes]
@@ -209,21 +215,78 @@ def time_sequence(r, args, scenes, opts):
         frames[i].pixels = b.data_ptr()
     seq = r.sequence(cs, frames, opts)
     stream = torch.cuda.ExternalStream(r.stream)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         seq.launch()
     stream.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(args.steps):
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in evs:
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        a.record(stream)
         seq.launch()
-    b.record(stream)
-    b.synchronize()
-    ms = a.elapsed_time(b) / args.steps
+        b.record(stream)
+    stream.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
     st = seq.stats()
     seq.close()
     rays = sum(s.camera.width() * s.camera.height() for s in scenes)
     return {"mrays_per_s": round(rays / (ms * 1e-3) / 1e6, 3), "ms_per_step": round(ms, 3),
-            "steps_per_ray": round(st.steps / max(1, st.rays), 1)}
+            "steps_per_ray": round(st.steps / max(1, st.rays), 1), "timed_steps": steps,
+            "band_rays": int(st.band_rays), "band_steps": int(st.band_steps), "fp32_steps": int(st.steps - st.band_steps)}
+
+
+class OracleErrors:
+    """Errors of GPU renders against the FP64 CPU oracle (RK4, step 0.01) on
+    seeded pixel samples: class mismatches, and the deflection of escaped rays
+    and hit radius of disc rays where the classes agree."""
+
+    def __init__(self):
+        self.n = 0
+        self.mismatch = 0
+        self.defl: list = []
+        self.radius: list = []
+        self.b: list = []
+
+    def add(self, scene, cls_img, aux_img, pts, threads, **oracle_kw):
+        import numpy as np
+
+        from blackhole_8_gb300 import capi
+        from oracle import oracle
+        pts = np.ascontiguousarray(pts, dtype=np.int32)
+        xs, ys = pts[:, 0], pts[:, 1]
+        o = oracle.render_rk4(scene, pixels=pts, threads=threads, **oracle_kw)
+        cls, aux = cls_img[ys, xs], aux_img[ys, xs]
+        agree = cls == o["cls"]
+        esc = agree & (o["cls"] == capi.CLASS_MISS)
+        dsk = agree & (o["cls"] == capi.CLASS_DISC)
+        self.n += len(xs)
+        self.mismatch += int((~agree).sum())
+        self.defl.append(np.abs(aux[esc] - o["aux"][esc]))
+        self.b.append(o["b_over_m"][esc])
+        self.radius.append(np.abs(aux[dsk] - o["aux"][dsk]))
+
+    def summary(self, by_b=False) -> dict:
+        import numpy as np
+        d = np.concatenate(self.defl) if self.defl else np.zeros(0)
+        r = np.concatenate(self.radius) if self.radius else np.zeros(0)
+
+        def q(a, p):
+            return float(np.quantile(a, p)) if len(a) else 0.0
+        out = {"pixels": self.n, "class_mismatch": self.mismatch / max(1, self.n), "escaped": int(len(d)),
+               "deflection_max_rad": float(d.max(initial=0)), "deflection_p999_rad": q(d, 0.999),
+               "disc_hits": int(len(r)), "hit_radius_max_M": float(r.max(initial=0)),
+               "hit_radius_p999_M": q(r, 0.999)}
+        if by_b and len(d):
+            db = np.abs(np.concatenate(self.b) - 3.0 * 3.0 ** 0.5)
+            bins = {}
+            edges = [0.0, 1e-10, 1e-8, 1e-7, 1e-6, 1e-5, 1e-4, 1e-3, 1e-2, 1e-1]
+            for lo, hi in zip(edges[:-1], edges[1:]):
+                sel = (db >= lo) & (db < hi)
+                if sel.any():
+                    bins[f"[{lo:g},{hi:g})"] = {"rays": int(sel.sum()), "deflection_max_rad": float(d[sel].max())}
+            out["deflection_by_abs_b_minus_bc_M"] = bins
+        return out
 
 
 def multi_leg(r, args, cpu: bool):
@@ -381,6 +444,127 @@ def adjoint_leg(r, args):
                             "FP64 central differences (h=1e-5) per parameter to 1e-3"}
 
 
+NEAR_CRITICAL_STEPS = 20000
+
+
+def near_critical_leg(r, args, flush, threads):
+    """The near-critical stress workloads, RK4 at the oracle's step 0.01 with
+    at most 20000 steps:
+    - photon ring: 4096x4096, FoV 0.5 deg aimed at the photon ring; the mixed
+      tracer (default band 5e-4 M) and plain FP32, timed as captured
+      sequences, with errors against the FP64 CPU oracle on every ray of the
+      FP64 band and 4000 seeded others;
+    - impact-parameter grid: 4096x4096 rays with b uniform over
+      3 sqrt(3) M +- 1e-4 M; the mixed tracer with the default band (every ray
+      in FP64) and with band 0 (FP32 with the FP64 first integral and the
+      energy projection), with errors on 20000 seeded rays binned by
+      |b - b_c|."""
+    import numpy as np
+
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+
+    out = {}
+    ring = S.photon_ring_scene(4096)
+    mixed = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
+                                 max_steps=NEAR_CRITICAL_STEPS)
+    plain = capi.default_options(precision=capi.PRECISION_FP32, max_steps=NEAR_CRITICAL_STEPS)
+    band_px = []
+    for y0 in range(0, 4096, 512):
+        ys, xs = np.mgrid[y0:y0 + 512, 0:4096]
+        b = S.ref_impact_parameter(ring, xs, ys)
+        sel = np.abs(b - 3.0 * 3.0 ** 0.5) < mixed.band
+        band_px.append(np.stack([xs[sel], ys[sel]], 1))
+    rng = np.random.default_rng(4)
+    pts = np.concatenate(band_px + [np.stack([rng.integers(0, 4096, 4000), rng.integers(0, 4096, 4000)], 1)])
+    leg = {"workload": "photon ring 4096x4096, FoV 0.5 deg at r = 20 M, b within ~0.085 M of 3 sqrt(3) M, "
+                       f"RK4 step 0.01, <= {NEAR_CRITICAL_STEPS} steps",
+           "sample": f"every FP64-band ray ({sum(len(p) for p in band_px)}) + 4000 seeded rays"}
+    for name, o in (("mixed", mixed), ("plain_fp32", plain)):
+        t = time_sequence(r, args, [ring], o, flush=flush)
+        fb = r.render([ring], o, hit_class=True, aux=True)[0]
+        st = r.stats()
+        err = OracleErrors()
+        err.add(ring, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
+        t.update({"band": o.band if name == "mixed" else None, "band_fraction": st.band_rays / st.rays,
+                  "errors_vs_cpu_oracle": err.summary(by_b=True)})
+        leg[name] = t
+    out["photon_ring"] = leg
+
+    grid = S.impact_grid_scene(4096)
+    rng = np.random.default_rng(5)
+    pts = np.stack([rng.integers(0, 4096, 20000), rng.integers(0, 4096, 20000)], 1)
+    leg = {"workload": "impact-parameter grid 4096x4096, b uniform over 3 sqrt(3) M +- 1e-4 M, RK4 step 0.01, "
+                       f"<= {NEAR_CRITICAL_STEPS} steps", "sample": "20000 seeded rays"}
+    for name, band in (("mixed_band_default", mixed.band), ("mixed_band_0", 0.0)):
+        o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
+                                 max_steps=NEAR_CRITICAL_STEPS, band=band)
+        steps = max(1, min(args.steps, 3))
+        t = time_sequence(r, args, [grid], o, steps=steps, warmup=1, flush=flush)
+        fb = r.render([grid], o, hit_class=True, aux=True)[0]
+        st = r.stats()
+        err = OracleErrors()
+        err.add(grid, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
+        t.update({"band": band, "band_fraction": st.band_rays / st.rays, "errors_vs_cpu_oracle": err.summary(by_b=True)})
+        leg[name] = t
+    out["impact_grid"] = leg
+    return out
+
+
+def batch_leg(r, args, flush, threads, fp32_peak):
+    """256 uneven scenes (sides log-uniform 64-1024, M, camera, FoV and disc
+    per scene, textures from a per-scene seed) in one persistent launch with
+    the autotuner's choice, timed as a captured sequence; roofline fraction
+    of its FP32 pass; steps per ray per scene (each scene rendered on its
+    own, outside the timed region); errors against the FP64 CPU oracle on 300
+    seeded pixels of every scene."""
+    import numpy as np
+
+    from blackhole_8_gb300 import capi
+    from blackhole_8_gb300 import scene as S
+
+    t0 = time.perf_counter()
+    scenes = S.batched_scenes(256)
+    build_s = time.perf_counter() - t0
+    cs = r.c_scenes(scenes)
+    t0 = time.perf_counter()
+    tuned, rep = r.autotune(cs, capi.default_options(), max_error=MAX_DEFLECTION_ERROR)
+    tune_s = time.perf_counter() - t0
+    t = time_sequence(r, args, scenes, tuned, flush=flush)
+    rays = sum(s.camera.width() * s.camera.height() for s in scenes)
+    achieved = t["fp32_steps"] * capi.RK4_ALGO_FLOPS_PER_STEP / (t["ms_per_step"] * 1e-3) / 1e12
+    per_scene = []
+    for sc in scenes:
+        r.render([sc], tuned)
+        st = r.stats()
+        per_scene.append(st.steps / max(1, st.rays))
+    per_scene = np.array(per_scene)
+    out = r.render(scenes, tuned, hit_class=True, aux=True)
+    err = OracleErrors()
+    rng = np.random.default_rng(6)
+    for sc, fb in zip(scenes, out):
+        w, h = sc.camera.width(), sc.camera.height()
+        err.add(sc, fb.hit_class, fb.aux, np.stack([rng.integers(0, w, 300), rng.integers(0, h, 300)], 1), threads)
+    t.update({"workload": f"256 scenes, sides 64-1024 log-uniform ({rays / 1e6:.1f} M rays), M 0.5-2, r_cam 6-50 M, "
+                          "incl 0-90 deg, FoV 20-90 deg, disc 6 M to 12-30 M, per-scene seeded textures",
+              "tuned": {"step": tuned.step, "band": tuned.band,
+                        "schedule": "persistent" if tuned.schedule == capi.SCHEDULE_PERSISTENT else "grid",
+                        "threads_per_block": tuned.threads_per_block, "refill_threshold": tuned.refill_threshold,
+                        "slice_steps": tuned.slice_steps, "block": [tuned.block_x, tuned.block_y],
+                        "rays_per_thread": tuned.rays_per_thread,
+                        "autotune_seconds": round(tune_s, 2), "candidates": rep.candidates},
+              "build_seconds": round(build_s, 1),
+              "band_fraction": t["band_rays"] / rays,
+              "steps_per_ray_per_scene": {"min": round(float(per_scene.min()), 1),
+                                          "median": round(float(np.median(per_scene)), 1),
+                                          "max": round(float(per_scene.max()), 1)},
+              "roofline": {"achieved_tflops": round(achieved, 3), "peak_tflops": round(fp32_peak, 3),
+                           "frac": round(achieved / fp32_peak, 4)},
+              "errors_vs_cpu_oracle": err.summary()})
+    return t
+
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import torch
@@ -413,10 +597,12 @@ def run_ours(args):
 
     launches = 0
 
-    def time_steps(opts, kernels_per_step, graph):
+    def time_steps(opts, kernels_per_step, graph, steps=None):
         """Times one batched render of the 120 frames per step: a replay of
-        the captured sequence (graph) or one bh_render_device call."""
+        the captured sequence (graph) or one bh_render_device call; `steps`
+        timed steps (default the run's K)."""
         nonlocal launches
+        steps = args.steps if steps is None else steps
         if graph:
             seq = r.sequence(cs, frames, opts)
             launch, stats = seq.launch, seq.stats
@@ -427,7 +613,7 @@ def run_ours(args):
             launch()
         stream.synchronize()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
+               for _ in range(steps)]
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
@@ -445,7 +631,7 @@ def run_ours(args):
         st = stats()
         if seq is not None:
             seq.close()
-        launches += kernels_per_step * args.steps
+        launches += kernels_per_step * steps
         return max_over_ranks(ms, world), st, wall
 
     fp32_tflops, sm_count = r.fp32_peak()
@@ -463,21 +649,33 @@ def run_ours(args):
     # MIXED launches five kernels per render (band classification, the band
     # list's sort, the FP64 band pass, the FP32 pass it launches from the
     # device, the host's draining FP32 launch), the plain tracer one.
-    ms_tuned, st_tuned, wall_tuned = time_steps(tuned, 5, graph=True)
+    tuned_kernels = 5 if tuned.schedule == capi.SCHEDULE_PERSISTENT else 1
+    ms_tuned, st_tuned, wall_tuned = time_steps(tuned, tuned_kernels, graph=True)
     eq = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
-    for name, opts, k, graph in [
-        ("mixed_batched_tuned_direct", tuned, 5, False),
-        ("mixed_batched_step0.01", eq, 5, True),
-        ("plain_fp32_grid", capi.default_options(precision=capi.PRECISION_FP32), 1, True),
+    plain_tuned = capi.default_options(precision=capi.PRECISION_FP32, step=tuned.step)
+    slow = max(1, min(args.steps, 3))  # the FP64 trapezoid takes ~1 s per fly-through
+    variant_opts = {}
+    for name, opts, k, graph, steps in [
+        ("mixed_batched_tuned_direct", tuned, tuned_kernels, False, None),
+        ("mixed_batched_step0.01", eq, 5, True, None),
+        ("plain_fp32_grid", capi.default_options(precision=capi.PRECISION_FP32), 1, True, None),
+        ("plain_fp32_grid_tuned_step", plain_tuned, 1, True, None),
         ("plain_fp32_persistent", capi.default_options(precision=capi.PRECISION_FP32,
-                                                       schedule=capi.SCHEDULE_PERSISTENT), 1, True),
+                                                       schedule=capi.SCHEDULE_PERSISTENT), 1, True, None),
+        ("reference_trapezoid_fp64", capi.default_options(integrator=capi.INTEGRATOR_REF_TRAPEZOID,
+                                                          precision=capi.PRECISION_FP64), 1, True, slow),
+        ("reference_trapezoid_fp32", capi.default_options(integrator=capi.INTEGRATOR_REF_TRAPEZOID), 1, True,
+         None),
     ]:
-        ms, st, wall = time_steps(opts, k, graph)
+        ms, st, wall = time_steps(opts, k, graph, steps)
         fp32_steps = st.steps - st.band_steps
+        variant_opts[name] = opts
         variants[name] = {"call": "bh_sequence_launch" if graph else "bh_render_device",
                           "mrays_per_s": round(job_throughput(rays_step, world, ms * 1e-3), 3),
-                          "ms_per_step": round(ms, 3), "step": opts.step, "steps_total": int(st.steps),
-                          "band_rays": int(st.band_rays),
+                          "ms_per_step": round(ms, 3), "timed_steps": steps or args.steps,
+                          "integrator": "reference trapezoid 20+20" if opts.integrator == capi.INTEGRATOR_REF_TRAPEZOID
+                          else "RK4", "step": opts.step if opts.integrator == capi.INTEGRATOR_RK4 else None,
+                          "steps_total": int(st.steps), "band_rays": int(st.band_rays),
                           "fp32_tflops": round(fp32_steps * capi.RK4_FLOPS_PER_STEP / (ms * 1e-3) / 1e12, 3),
                           "wall_s": round(wall, 3)}
     clock_info = clocks.stop()
@@ -491,8 +689,10 @@ def run_ours(args):
     issue_frac = fp32_steps * capi.RK4_INSTRUCTIONS_PER_STEP / (ms_tuned * 1e-3) / (fp32_tflops * 1e12 / 2)
     variants["mixed_batched_tuned"] = {
         "call": "bh_sequence_launch", "mrays_per_s": round(value, 3), "ms_per_step": round(ms_tuned, 3), "step": tuned.step,
-        "band": tuned.band, "threads_per_block": tuned.threads_per_block,
-        "refill_threshold": tuned.refill_threshold, "slice_steps": tuned.slice_steps,
+        "band": tuned.band, "schedule": "persistent" if tuned.schedule == capi.SCHEDULE_PERSISTENT else "grid",
+        "threads_per_block": tuned.threads_per_block, "refill_threshold": tuned.refill_threshold,
+        "slice_steps": tuned.slice_steps, "block": [tuned.block_x, tuned.block_y],
+        "rays_per_thread": tuned.rays_per_thread,
         "steps_total": int(st_tuned.steps), "band_rays": int(st_tuned.band_rays),
         "band_fraction": st_tuned.band_rays / rays_step, "band_steps": int(st_tuned.band_steps),
         "wall_s": round(wall_tuned, 3)}
@@ -514,7 +714,7 @@ def run_ours(args):
         for _ in range(args.steps):
             r.render_into(cs, hframes, e2e_opts)
         dt = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
-        launches += 5 * args.steps
+        launches += tuned_kernels * args.steps
         st_e2e = r.stats()
         e2e = {"value": round(job_throughput(rays_step, world, dt), 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
@@ -528,6 +728,33 @@ def run_ours(args):
     if not args.no_objects:
         objects = objects_leg(r, args, cpu=rank == 0 and not args.no_cpu)
         objects["multi_holes"] = multi_leg(r, args, cpu=rank == 0 and not args.no_cpu)
+
+    # errors against the FP64 CPU oracle on 4000 seeded pixels of frames
+    # 0/39/79/119 (outside the timed region): the tuned mixed tracer, the
+    # mixed tracer at step 0.01 and plain FP32 at the tuned step
+    import numpy as np
+    threads = os.cpu_count() or 1
+    accuracy = {}
+    picks = [0, 39, 79, 119]
+    for name, opts in (("mixed_batched_tuned", tuned), ("mixed_batched_step0.01", eq),
+                       ("plain_fp32_grid_tuned_step", plain_tuned)):
+        err = OracleErrors()
+        rng = np.random.default_rng(11)
+        outs = r.render([scenes[i] for i in picks], opts, hit_class=True, aux=True)
+        for i, fb in zip(picks, outs):
+            pts = np.stack([rng.integers(0, WIDTH, 4000), rng.integers(0, HEIGHT, 4000)], 1)
+            err.add(scenes[i], fb.hit_class, fb.aux, pts, threads)
+        accuracy[name] = err.summary(by_b=True)
+    accuracy["vs"] = ("FP64 CPU oracle (RK4, step 0.01), 4000 seeded pixels of each of frames 0/39/79/119; "
+                      "errors where the classes agree")
+    accuracy["autotune_vs_gpu_fp64"] = {"max_deflection_rad": rep.max_deflection,
+                                        "max_hit_radius_error_M": rep.max_radius_error,
+                                        "class_mismatch": rep.class_mismatch}
+
+    near_critical = batch = None
+    if not args.no_stress:
+        near_critical = near_critical_leg(r, args, flush, threads)
+        batch = batch_leg(r, args, flush, threads, fp32_tflops)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -543,10 +770,7 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "frames": FRAMES, "width": WIDTH, "height": HEIGHT,
                        "tracer": "mixed-precision batched, autotuned", "max_deflection_error_rad": MAX_DEFLECTION_ERROR,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
-            "accuracy": {"max_deflection_rad": rep.max_deflection, "max_hit_radius_error_M": rep.max_radius_error,
-                         "class_mismatch": rep.class_mismatch,
-                         "vs": "FP64 render (RK4, step 0.01) of frames 0/39/79/119; that path matches the CPU "
-                               "FP64 oracle in tests"},
+            "accuracy": accuracy,
             "autotune": {"step": tuned.step, "candidates": rep.candidates, "seconds": round(tune_s, 2)},
             "variants": variants,
             "roofline": {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_tflops, 3),
@@ -558,7 +782,7 @@ def run_ours(args):
                          "instructions_per_step": capi.RK4_INSTRUCTIONS_PER_STEP, "sm_count": sm_count,
                          "fp64_peak_tflops_measured": round(fp64_tflops, 3)},
             "clocks": clock_info, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu,
-            "adjoint": adjoint, "objects": objects}))
+            "adjoint": adjoint, "objects": objects, "near_critical": near_critical, "batch_256": batch}))
     r.close()
     if world > 1:
         import torch.distributed as dist
