@@ -78,7 +78,8 @@ class RenderOptions(C.Structure):
                 ("block_x", C.c_int32), ("block_y", C.c_int32), ("threads_per_block", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("refill_threshold", C.c_int32),
                 ("band_step", C.c_double), ("setup_band", C.c_double), ("slice_steps", C.c_int32),
-                ("band_lanes", C.c_int32), ("band_serial", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("band_lanes", C.c_int32), ("band_serial", C.c_int32), ("rays_per_thread", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class RenderStats(C.Structure):

@@ -184,6 +184,7 @@ void resolve_defaults(const bh_render_options* in, bh_render_options* out) {
   if (out->setup_band < 0) out->setup_band = d.setup_band;
   if (out->slice_steps == 0) out->slice_steps = d.slice_steps;
   if (out->band_lanes == 0) out->band_lanes = d.band_lanes;
+  if (out->rays_per_thread == 0) out->rays_per_thread = d.rays_per_thread;
 }
 
 int validate_options(bh_ctx* ctx, const bh_render_options& o) {
@@ -510,6 +511,7 @@ LaunchParams base_params(const bh_render_options& o) {
   p.slice_steps = o.slice_steps;
   p.band_lanes = o.band_lanes;
   p.band_serial = o.band_serial;
+  p.rays_per_thread = o.rays_per_thread > 0 ? o.rays_per_thread : 1;
   return p;
 }
 
@@ -634,6 +636,7 @@ void bh_default_options(bh_render_options* o) {
   o->threads_per_block = 256;
   o->blocks_per_sm = 0;
   o->refill_threshold = 32;
+  o->rays_per_thread = 1;
 }
 
 int bh_create(bh_ctx** out, int device) {
@@ -1117,15 +1120,19 @@ bool cache_lookup(const char* path, const std::string& key, bh_render_options* o
   while (std::fgets(line, sizeof(line), f)) {
     char k[600];
     double step, band, defl, rad, mis, ms;
-    int threads, refill, slice;
-    if (std::sscanf(line, "%599s %lf %lf %d %d %d %lf %lf %lf %lf", k, &step, &band, &threads, &refill, &slice,
-                    &defl, &rad, &mis, &ms) == 10 &&
+    int threads, refill, slice, schedule, bx, by, rpt;
+    if (std::sscanf(line, "%599s %lf %lf %d %d %d %d %d %d %d %lf %lf %lf %lf", k, &step, &band, &threads, &refill,
+                    &slice, &schedule, &bx, &by, &rpt, &defl, &rad, &mis, &ms) == 14 &&
         key == k) {
       o->step = step;
       o->band = band;
       o->threads_per_block = threads;
       o->refill_threshold = refill;
       o->slice_steps = slice;
+      o->schedule = schedule;
+      o->block_x = bx;
+      o->block_y = by;
+      o->rays_per_thread = rpt;
       rep->step = step;
       rep->max_deflection = defl;
       rep->max_radius_error = rad;
@@ -1142,9 +1149,9 @@ void cache_store(const char* path, const std::string& key, const bh_render_optio
   if (!path) return;
   FILE* f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%s %.17g %.17g %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), o.step, o.band,
-               o.threads_per_block, o.refill_threshold, o.slice_steps, rep.max_deflection, rep.max_radius_error,
-               rep.class_mismatch, rep.kernel_ms);
+  std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), o.step, o.band,
+               o.threads_per_block, o.refill_threshold, o.slice_steps, o.schedule, o.block_x, o.block_y,
+               o.rays_per_thread, rep.max_deflection, rep.max_radius_error, rep.class_mismatch, rep.kernel_ms);
   std::fclose(f);
 }
 
@@ -1237,6 +1244,22 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
   }
   double best = 1e30;
   bh_render_options best_o = chosen;
+  auto time_candidate = [&](const bh_render_options& c) -> int {
+    double ms = 1e30;
+    for (int rep = 0; rep < 2; ++rep) {
+      if ((rc = render_on_device(ctx, scenes, n, bf.data(), c, ctx->stream))) return rc;
+      bh_render_stats st;
+      if ((rc = bh_get_stats(ctx, &st))) return rc;
+      ms = std::min(ms, st.kernel_ms);
+    }
+    report->candidates++;
+    if (ms < best) {
+      best = ms;
+      best_o = c;
+    }
+    return BH_OK;
+  };
+  // the persistent schedule: band, block size, refill threshold, slice
   for (double band : {5e-4, 1e-3})
     for (int threads : {128, 256})
       for (int refill : {16, 32})
@@ -1247,19 +1270,22 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
           c.refill_threshold = refill;
           c.slice_steps = slice;
           c.format = BH_FORMAT_BGRA8;
-          double ms = 1e30;
-          for (int rep = 0; rep < 2; ++rep) {
-            if ((rc = render_on_device(ctx, scenes, n, bf.data(), c, ctx->stream))) return rc;
-            bh_render_stats st;
-            if ((rc = bh_get_stats(ctx, &st))) return rc;
-            ms = std::min(ms, st.kernel_ms);
-          }
-          report->candidates++;
-          if (ms < best) {
-            best = ms;
-            best_o = c;
-          }
+          if ((rc = time_candidate(c))) return rc;
         }
+  // the grid schedule (band rays traced inline): block shape and rays per
+  // thread
+  static const int kShapes[][2] = {{8, 16}, {16, 8}, {32, 4}, {8, 8}, {16, 16}};
+  for (const auto& sh : kShapes)
+    for (int rpt : {1, 2, 4}) {
+      bh_render_options c = chosen;
+      c.schedule = BH_SCHEDULE_GRID;
+      c.band = std::max(5e-4, base.band);
+      c.block_x = sh[0];
+      c.block_y = sh[1];
+      c.rays_per_thread = rpt;
+      c.format = BH_FORMAT_BGRA8;
+      if ((rc = time_candidate(c))) return rc;
+    }
   best_o.format = opts->format;
   report->kernel_ms = best;
   *opts = best_o;

@@ -179,6 +179,7 @@ struct LaunchParams {
   int32_t band_lanes;
   int32_t band_serial;        // persistent MIXED: 1 = FP32 pass, then FP64 pass, from the host
   int32_t mixed_blocks;       // persistent MIXED: grid of the FP32 pass the FP64 pass launches (0: none)
+  int32_t rays_per_thread;    // GRID: consecutive block tiles down the image per block (>= 1)
 };
 
 // Bound on how much b / M changes between neighbouring pixels of a row. The
@@ -360,6 +361,8 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
   if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64) return bad(BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
   if (o.refill_threshold < 1 || o.refill_threshold > 32)
     return bad(BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");
+  if (o.rays_per_thread < 0 || o.rays_per_thread > 8)
+    return bad(BH_ERR_INVALID_ARGUMENT, "rays_per_thread must be in [0, 8]");
   return BH_OK;
 }
 

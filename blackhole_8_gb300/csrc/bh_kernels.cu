@@ -219,6 +219,13 @@ struct Hit {
 
 __device__ __forceinline__ Hit miss_hit() { return {make_uchar4(0, 0, 0, 255), BH_CLASS_MISS, 0.f}; }
 
+// Class and aux outputs of pixel (x, y), where the frame asks for them.
+__device__ __forceinline__ void store_extras(const DevScene& s, int x, int y, const Hit& h) {
+  const long long pix = (long long)y * s.width + x;
+  if (s.cls) s.cls[pix] = (uint8_t)h.cls;
+  if (s.aux) s.aux[pix] = h.aux;
+}
+
 __device__ __forceinline__ void store_hit(const DevScene& s, int format, int x, int y, const Hit& h) {
   const long long pix = (long long)y * s.width + x;
   uchar4 c = h.bgra;
@@ -1230,48 +1237,116 @@ __device__ __forceinline__ unsigned lane_id() {
   return l;
 }
 
+// Sums v over the active lanes into *dst: two 32-bit warp reductions, of the
+// low 27 bits and of the rest, exact for every v below 2^54 (a thread's step
+// count stays below 8 * 1e8 < 2^30).
 __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
   const unsigned m = __activemask();
-  unsigned lo = (unsigned)min(v, 0xffffffffull);
-  lo = __reduce_add_sync(m, lo);
-  if (lane_id() == unsigned(__ffs(m) - 1) && lo) atomicAdd(dst, (unsigned long long)lo);
+  const unsigned lo = __reduce_add_sync(m, unsigned(v & 0x7ffffffull));
+  const unsigned hi = __reduce_add_sync(m, unsigned(v >> 27));
+  const unsigned long long t = (unsigned long long)lo + ((unsigned long long)hi << 27);
+  if (lane_id() == unsigned(__ffs(m) - 1) && t) atomicAdd(dst, t);
 }
 
-// GRID schedule: one thread per pixel, gridDim.z = scene; one kernel per
-// precision and integrator, each with the registers (and the occupancy) of
-// its own variant.
+// BGR8 (CV_8UC3) frames. A warp whose 32 lanes hold the pixels of one block
+// of the frame -- rows of bw pixels (4, 8, 16 or 32), lane l at
+// (x0 + l % bw, y0 + l / bw) -- writes the block's 96 bytes as 24 32-bit
+// words, four pixels to three words, where byte stores would take 96 store
+// instructions per warp. `bgr` is the lane's pixel as B | G << 8 | R << 16;
+// word w of a row holds the bytes 4w .. 4w+3 of the row, which come from at
+// most two pixels. Every row must start on a 4-byte boundary (frame base
+// 4-aligned, width and x0 multiples of 4). Called by all 32 lanes.
+__device__ __forceinline__ void store_bgr8_words(uint8_t* frame, int width, int x0, int y0, int bw, uint32_t bgr) {
+  const int lane = int(lane_id());
+  const int wpr = (3 * bw) >> 2;  // words per row
+  const int r = lane / wpr, w = lane - r * wpr;
+  const int k = w % 3;
+  const int src = r * bw + 4 * (w / 3) + k;  // the pixel of the word's first byte
+  const uint32_t a = __shfl_sync(kFull, bgr, src & 31);
+  const uint32_t b = __shfl_sync(kFull, bgr, (src + 1) & 31);
+  if (lane < 24)
+    reinterpret_cast<uint32_t*>(frame + 3 * ((long long)(y0 + r) * width + x0))[w] =
+        (a >> (8 * k)) | (b << (24 - 8 * k));
+}
+
+__device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
+  return uint32_t(h.bgra.x) | (uint32_t(h.bgra.y) << 8) | (uint32_t(h.bgra.z) << 16);
+}
+
+// True when the warp's pixels ((x, y) per lane, `valid` where it lies in the
+// frame) form a block of rows of bw pixels starting at lane 0's pixel that
+// store_bgr8_words can write. Called by all 32 lanes; the result is the
+// same on every lane.
+__device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, bool valid, int bw) {
+  const int lane = int(lane_id());
+  const int x0 = __shfl_sync(kFull, x, 0), y0 = __shfl_sync(kFull, y, 0);
+  const bool mine = valid && x == x0 + lane % bw && y == y0 + lane / bw;
+  return __all_sync(kFull, mine) && (x0 & 3) == 0 && (s.width & 3) == 0 &&
+         (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
+}
+
+// GRID store of pixel (x, y) (`valid`: it lies in the frame). In BGR8 frames
+// a warp of a block whose rows are whole warps or hold a whole number of
+// warp rows writes packed words. Called by all 32 lanes of the warp.
+__device__ __forceinline__ void grid_store(const DevScene& s, int format, int x, int y, bool valid, const Hit& h) {
+  if (format == BH_FORMAT_BGR8) {
+    const int bx = int(blockDim.x), bw = bx < 32 ? bx : 32;
+    if ((bx % 32 == 0 || 32 % bx == 0) && (bw & 3) == 0 && bgr8_block_ok(s, x, y, valid, bw)) {
+      store_bgr8_words(s.pixels, s.width, __shfl_sync(kFull, x, 0), __shfl_sync(kFull, y, 0), bw, bgr_word(h));
+      store_extras(s, x, y, h);
+      return;
+    }
+  }
+  if (valid) store_hit(s, format, x, y, h);
+}
+
+// GRID schedule: one thread per pixel of each of rays_per_thread block tiles
+// (consecutive down the image, traced one after the other), gridDim.z =
+// scene; one kernel per precision and integrator, each with the registers
+// (and the occupancy) of its own variant.
 template <int kPrecision, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   const DevScene& s = p.scenes[blockIdx.z];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= s.width || y >= s.height) return;
-  Hit h;
-  int steps = 0;
-  int band_ray = 0;
-  if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
-    h = kPrecision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
-  } else if (kPrecision == BH_PRECISION_FP64) {
-    h = trace_rk4<double, false>(s, x, y, p.c64, &steps);
-  } else if (kPrecision == BH_PRECISION_MIXED) {
-    RayState<float> st;
-    if (setup_mixed(s, x, y, p, st)) {
-      steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
-      h = finish_rk4<float>(s, st, p.c32);
+  // every lane stays to the end: BGR8 stores are whole-warp operations
+  unsigned long long steps_all = 0, rays = 0, band_rays = 0, band_steps = 0;
+  for (int k = 0; k < p.rays_per_thread; ++k) {
+    const int row0 = (blockIdx.y * p.rays_per_thread + k) * blockDim.y;
+    if (row0 >= s.height) break;  // the same for the whole block
+    const int y = row0 + threadIdx.y;
+    const bool valid = x < s.width && y < s.height;
+    Hit h = miss_hit();
+    int steps = 0;
+    int band_ray = 0;
+    if (!valid) {
+    } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+      h = kPrecision == BH_PRECISION_FP64 ? trace_ref<double>(s, x, y) : trace_ref<float>(s, x, y);
+    } else if (kPrecision == BH_PRECISION_FP64) {
+      h = trace_rk4<double, false>(s, x, y, p.c64, &steps);
+    } else if (kPrecision == BH_PRECISION_MIXED) {
+      RayState<float> st;
+      if (setup_mixed(s, x, y, p, st)) {
+        steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
+        h = finish_rk4<float>(s, st, p.c32);
+      } else {
+        band_ray = 1;
+        h = trace_band(s, x, y, p, &steps);
+      }
     } else {
-      band_ray = 1;
-      h = trace_band(s, x, y, p, &steps);
+      h = trace_rk4<float, false>(s, x, y, p.c32, &steps);
     }
-  } else {
-    h = trace_rk4<float, false>(s, x, y, p.c32, &steps);
+    grid_store(s, p.format, x, y, valid, h);
+    steps_all += steps;
+    rays += valid ? 1 : 0;
+    band_rays += band_ray;
+    band_steps += band_ray ? steps : 0;
   }
-  store_hit(s, p.format, x, y, h);
   if (p.counters) {
-    warp_add(&p.counters->steps, (unsigned long long)steps);
-    warp_add(&p.counters->rays, 1ull);
-    if (__any_sync(__activemask(), band_ray)) {
-      warp_add(&p.counters->band_rays, (unsigned long long)band_ray);
-      warp_add(&p.counters->band_steps, band_ray ? (unsigned long long)steps : 0ull);
+    warp_add(&p.counters->steps, steps_all);
+    warp_add(&p.counters->rays, rays);
+    if (__any_sync(__activemask(), band_rays != 0)) {
+      warp_add(&p.counters->band_rays, band_rays);
+      warp_add(&p.counters->band_steps, band_steps);
     }
   }
 }
@@ -1286,25 +1361,34 @@ template <typename R, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   const DevScene& s = p.scenes[blockIdx.z];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= s.width || y >= s.height) return;
-  Hit h;
-  int steps = 0;
-  if (kIntegrator == BH_INTEGRATOR_FLAT) {
-    h = trace_flat<R>(s, x, y);
-  } else if (kIntegrator == BH_INTEGRATOR_MULTI) {
-    h = trace_multi<R>(s, x, y, bulk_consts<R>(p), &steps);
-  } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
-    h = trace_ref<R, true>(s, x, y);
-  } else if (s.n_objects > 0) {
-    h = trace_rk4_obj<R>(s, x, y, bulk_consts<R>(p), &steps);
-  } else {
-    h = trace_rk4<R, false>(s, x, y, bulk_consts<R>(p), &steps);
+  // every lane stays to the end: BGR8 stores are whole-warp operations
+  unsigned long long steps_all = 0, rays = 0;
+  for (int k = 0; k < p.rays_per_thread; ++k) {
+    const int row0 = (blockIdx.y * p.rays_per_thread + k) * blockDim.y;
+    if (row0 >= s.height) break;  // the same for the whole block
+    const int y = row0 + threadIdx.y;
+    const bool valid = x < s.width && y < s.height;
+    Hit h = miss_hit();
+    int steps = 0;
+    if (!valid) {
+    } else if (kIntegrator == BH_INTEGRATOR_FLAT) {
+      h = trace_flat<R>(s, x, y);
+    } else if (kIntegrator == BH_INTEGRATOR_MULTI) {
+      h = trace_multi<R>(s, x, y, bulk_consts<R>(p), &steps);
+    } else if (kIntegrator == BH_INTEGRATOR_REF_TRAPEZOID) {
+      h = trace_ref<R, true>(s, x, y);
+    } else if (s.n_objects > 0) {
+      h = trace_rk4_obj<R>(s, x, y, bulk_consts<R>(p), &steps);
+    } else {
+      h = trace_rk4<R, false>(s, x, y, bulk_consts<R>(p), &steps);
+    }
+    grid_store(s, p.format, x, y, valid, h);
+    steps_all += steps;
+    rays += valid ? 1 : 0;
   }
-  store_hit(s, p.format, x, y, h);
   if (p.counters) {
-    warp_add(&p.counters->steps, (unsigned long long)steps);
-    warp_add(&p.counters->rays, 1ull);
+    warp_add(&p.counters->steps, steps_all);
+    warp_add(&p.counters->rays, rays);
   }
 }
 
@@ -1549,14 +1633,30 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
         idle = __ballot_sync(kFull, st.status == kDone) & usable & ~given;
       }
     }
+    bool fin = false;
+    Hit hit = miss_hit();
     if (st.status != kDone) {
       const DevScene& s = p.scenes[scene];
       steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
       if (st.status != kRunning) {
-        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c));
+        hit = finish_rk4<R>(s, st, c);
+        fin = true;
         st.status = kDone;
       }
     }
+    if (kPass != 2 && p.format == BH_FORMAT_BGR8) {
+      // the lanes finishing one whole 8x4 tile together (a full refill's
+      // rays, lane l at pixel l of the tile) write it as packed words
+      const int sc0 = __shfl_sync(kFull, scene, 0);
+      const DevScene& s0 = p.scenes[sc0];
+      if (bgr8_block_ok(s0, px, py, fin && scene == sc0, 8)) {
+        store_bgr8_words(s0.pixels, s0.width, __shfl_sync(kFull, px, 0), __shfl_sync(kFull, py, 0), 8,
+                         bgr_word(hit));
+        store_extras(s0, px, py, hit);
+        continue;
+      }
+    }
+    if (fin) store_hit(p.scenes[scene], p.format, px, py, hit);
   }
   // per-warp totals
   unsigned long long wsteps = steps, wrays = rays;
@@ -1638,7 +1738,8 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
     max_h = scene_h[i] > max_h ? scene_h[i] : max_h;
   }
   const dim3 block(block_x, block_y, 1);
-  const dim3 grid((max_w + block_x - 1) / block_x, (max_h + block_y - 1) / block_y, p.n_scenes);
+  const int rows = block_y * std::max(1, p.rays_per_thread);  // image rows per block
+  const dim3 grid((max_w + block_x - 1) / block_x, (max_h + rows - 1) / rows, p.n_scenes);
   void (*kernel)(LaunchParams);
   const bool fp64 = p.precision == BH_PRECISION_FP64;
   if (!objects) {

@@ -282,6 +282,7 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
                    &p.band_tmp, &p.band_key);
   p.band_capacity = uint32_t(BH_NOALLOC_MAX_RAYS);
   p.refill_threshold = o.refill_threshold;
+  p.rays_per_thread = o.rays_per_thread > 0 ? o.rays_per_thread : 1;
   p.slice_steps = o.slice_steps;
   p.band_lanes = o.band_lanes;
   p.band_serial = o.band_serial;

@@ -245,7 +245,10 @@ typedef struct bh_render_options {
                                 and launches it from the device; 1 = the FP32
                                 pass, then the FP64 pass, both launched by the
                                 host (each pass on its own, e.g. to profile) */
-  int32_t reserved[3];
+  int32_t rays_per_thread;   /* GRID: pixels each thread traces, from that many
+                                consecutive block tiles down the image, one
+                                after the other (1..8; 0 = 1, the default) */
+  int32_t reserved[2];
 } bh_render_options;
 
 /* Counters of the most recent render on a context. */
@@ -314,17 +317,21 @@ void bh_sequence_destroy(bh_sequence* seq);
 
 /* ---- autotuner -----------------------------------------------------------------------
  * No counterpart in the reference. Chooses the mixed-precision batched
- * tracer's RK4 step, FP64 band width and persistent-schedule shape (block
- * size, refill threshold, slice length) for a batch of scenes:
+ * tracer's RK4 step, FP64 band width, schedule and its shape (persistent:
+ * block size, refill threshold, slice length; grid: block shape and rays per
+ * thread) for a batch of scenes:
  *   1. renders a sample of the scenes (up to 4, evenly spaced) in FP64 with
  *      the options' step as the reference (the oracle's scheme);
  *   2. takes the largest step in {0.1, 0.08, 0.05, 0.04, 0.03, 0.02, 0.01}
  *      whose MIXED render of the sample stays within max_error / 2 rad of the
  *      reference deflection on every escaped ray with an agreeing class, with
  *      classes agreeing on >= 99.99 % of pixels;
- *   3. times the schedule candidates on the whole batch and keeps the fastest.
+ *   3. times the schedule candidates on the whole batch and keeps the
+ *      fastest: PERSISTENT with band {5e-4, 1e-3} x threads {128, 256} x
+ *      refill {16, 32} x slice {128, 256, 512}, and GRID with block shapes
+ *      {8x16, 16x8, 32x4, 8x8, 16x16} x rays per thread {1, 2, 4}.
  * `opts` is read as the base (integrator must be RK4) and overwritten with
- * the choice (precision MIXED, schedule PERSISTENT). When cache_path is not
+ * the choice (precision MIXED). When cache_path is not
  * NULL the choice is looked up there first (key: device, batch shape,
  * max_error) and appended after tuning. The sample's renders and the timing
  * frames use the context's device buffers. */

@@ -131,6 +131,30 @@ def test_persistent_matches_grid(renderer, single):
     assert sa.rays == sb.rays and abs(int(sa.steps) - int(sb.steps)) <= 1e-4 * sa.steps
 
 
+@pytest.mark.parametrize("precision,integrator", [(capi.PRECISION_MIXED, capi.INTEGRATOR_RK4),
+                                                  (capi.PRECISION_FP32, capi.INTEGRATOR_RK4),
+                                                  (capi.PRECISION_FP64, capi.INTEGRATOR_REF_TRAPEZOID)],
+                         ids=["mixed", "fp32", "trapezoid-fp64"])
+def test_grid_shape_and_rays_per_thread_change_nothing(renderer, precision, integrator):
+    """The GRID schedule's block shape and rays per thread only change which
+    thread traces a pixel: frames, classes and counters are identical (two
+    frames of different sizes, so that block tiles overhang the images)."""
+    scenes = [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1]]
+    ref, ref_st = None, None
+    for bx, by, rpt in [(8, 16, 1), (8, 16, 2), (16, 8, 4), (32, 4, 3), (8, 8, 8), (16, 16, 1)]:
+        o = opts(precision=precision, integrator=integrator, block_x=bx, block_y=by, rays_per_thread=rpt)
+        out = renderer.render(scenes, o, hit_class=True)
+        st = renderer.stats()
+        if ref is None:
+            ref, ref_st = out, st
+            continue
+        for a, b in zip(ref, out):
+            assert np.array_equal(a.pixels, b.pixels) and np.array_equal(a.hit_class, b.hit_class), (bx, by, rpt)
+        assert (st.rays, st.steps, st.band_rays, st.band_steps) == \
+            (ref_st.rays, ref_st.steps, ref_st.band_rays, ref_st.band_steps), (bx, by, rpt)
+    assert ref_st.rays == 200 * 117 + 150 * 83
+
+
 def test_step_counts_match_oracle(renderer):
     sc = S.single_scene(96, 54)
     o = oracle.render_rk4(sc)
@@ -138,6 +162,29 @@ def test_step_counts_match_oracle(renderer):
     st = renderer.stats()
     assert st.rays == 96 * 54
     assert abs(int(st.steps) - int(o["steps"].sum())) <= 2
+
+
+@pytest.mark.parametrize("schedule,precision,bx,by", [
+    (capi.SCHEDULE_PERSISTENT, capi.PRECISION_MIXED, 8, 16), (capi.SCHEDULE_PERSISTENT, capi.PRECISION_FP32, 8, 16),
+    (capi.SCHEDULE_GRID, capi.PRECISION_FP32, 8, 16), (capi.SCHEDULE_GRID, capi.PRECISION_FP32, 16, 8),
+    (capi.SCHEDULE_GRID, capi.PRECISION_MIXED, 32, 4), (capi.SCHEDULE_GRID, capi.PRECISION_FP32, 4, 8),
+    (capi.SCHEDULE_GRID, capi.PRECISION_FP32, 64, 2), (capi.SCHEDULE_GRID, capi.PRECISION_FP32, 12, 8)],
+    ids=["persistent-mixed", "persistent-fp32", "grid-8x16", "grid-16x8", "grid-mixed-32x4", "grid-4x8",
+         "grid-64x2", "grid-12x8"])
+def test_bgr8_frames_equal_bgra8(renderer, schedule, precision, bx, by):
+    """BGR8 (CV_8UC3) frames, which whole warps write as packed 32-bit words
+    where the frame width allows it and byte by byte elsewhere, hold exactly
+    the BGRA8 frame's first three channels: widths that are multiples of 4
+    (packed) and not (bytes), image edges, several block shapes (12-wide
+    blocks do not map warps to rows and always take the byte path)."""
+    scenes = [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1], S.single_scene(64, 36)]
+    o = opts(schedule=schedule, precision=precision, block_x=bx, block_y=by, format=capi.FORMAT_BGRA8)
+    a = renderer.render(scenes, o, hit_class=True)
+    o.format = capi.FORMAT_BGR8
+    b = renderer.render(scenes, o, hit_class=True)
+    for fa, fb in zip(a, b):
+        assert np.array_equal(fa.pixels[..., :3], fb.pixels)
+        assert np.array_equal(fa.hit_class, fb.hit_class)
 
 
 def test_pixel_formats_agree(renderer):
