@@ -27,6 +27,7 @@ collective on the data path); value = all ranks' rays / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -43,6 +44,7 @@ WORKLOAD = "fly-through 120 frames 1920x1080, r 30M->8M spiral, incl 60->89 deg,
            "RK4 <=4000 steps, escape 100M"
 CPU_SAMPLE_FRAMES = list(range(0, FRAMES, 15))  # 8 frames
 MAX_DEFLECTION_ERROR = 1e-4
+SCHEDULE_NAMES = {0: "grid", 1: "persistent", 2: "hybrid"}
 
 
 def parse():
@@ -447,7 +449,7 @@ def adjoint_leg(r, args):
 NEAR_CRITICAL_STEPS = 20000
 
 
-def near_critical_leg(r, args, flush, threads):
+def near_critical_leg(r, args, flush, threads, tuned):
     """The near-critical stress workloads, RK4 at the oracle's step 0.01 with
     at most 20000 steps:
     - photon ring: 4096x4096, FoV 0.5 deg aimed at the photon ring; the mixed
@@ -456,9 +458,10 @@ def near_critical_leg(r, args, flush, threads):
       FP64 band and 4000 seeded others;
     - impact-parameter grid: 4096x4096 rays with b uniform over
       3 sqrt(3) M +- 1e-4 M; the mixed tracer with the default band (every ray
-      in FP64) and with band 0 (FP32 with the FP64 first integral and the
-      energy projection), with errors on 20000 seeded rays binned by
-      |b - b_c|."""
+      in FP64), with band 0 (FP32 with the FP64 first integral and the
+      energy projection) and with the fly-through's tuned step, band and
+      schedule, with errors on 20000 seeded rays binned by |b - b_c|.
+    The photon ring also runs with the tuned options."""
     import numpy as np
 
     from blackhole_8_gb300 import capi
@@ -480,13 +483,17 @@ def near_critical_leg(r, args, flush, threads):
     leg = {"workload": "photon ring 4096x4096, FoV 0.5 deg at r = 20 M, b within ~0.085 M of 3 sqrt(3) M, "
                        f"RK4 step 0.01, <= {NEAR_CRITICAL_STEPS} steps",
            "sample": f"every FP64-band ray ({sum(len(p) for p in band_px)}) + 4000 seeded rays"}
-    for name, o in (("mixed", mixed), ("plain_fp32", plain)):
+    tuned_nc = capi.RenderOptions()
+    C.memmove(C.byref(tuned_nc), C.byref(tuned), C.sizeof(tuned_nc))
+    tuned_nc.max_steps = NEAR_CRITICAL_STEPS
+    for name, o in (("mixed", mixed), ("mixed_tuned", tuned_nc), ("plain_fp32", plain)):
         t = time_sequence(r, args, [ring], o, flush=flush)
         fb = r.render([ring], o, hit_class=True, aux=True)[0]
         st = r.stats()
         err = OracleErrors()
         err.add(ring, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
-        t.update({"band": o.band if name == "mixed" else None, "band_fraction": st.band_rays / st.rays,
+        t.update({"band": o.band if o.precision == capi.PRECISION_MIXED else None, "step": o.step,
+                  "schedule": SCHEDULE_NAMES[o.schedule], "band_fraction": st.band_rays / st.rays,
                   "errors_vs_cpu_oracle": err.summary(by_b=True)})
         leg[name] = t
     out["photon_ring"] = leg
@@ -496,16 +503,20 @@ def near_critical_leg(r, args, flush, threads):
     pts = np.stack([rng.integers(0, 4096, 20000), rng.integers(0, 4096, 20000)], 1)
     leg = {"workload": "impact-parameter grid 4096x4096, b uniform over 3 sqrt(3) M +- 1e-4 M, RK4 step 0.01, "
                        f"<= {NEAR_CRITICAL_STEPS} steps", "sample": "20000 seeded rays"}
-    for name, band in (("mixed_band_default", mixed.band), ("mixed_band_0", 0.0)):
-        o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
-                                 max_steps=NEAR_CRITICAL_STEPS, band=band)
+    for name, band in (("mixed_band_default", mixed.band), ("mixed_band_0", 0.0), ("mixed_tuned", None)):
+        if band is None:
+            o = tuned_nc
+        else:
+            o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
+                                     max_steps=NEAR_CRITICAL_STEPS, band=band)
         steps = max(1, min(args.steps, 3))
         t = time_sequence(r, args, [grid], o, steps=steps, warmup=1, flush=flush)
         fb = r.render([grid], o, hit_class=True, aux=True)[0]
         st = r.stats()
         err = OracleErrors()
         err.add(grid, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
-        t.update({"band": band, "band_fraction": st.band_rays / st.rays, "errors_vs_cpu_oracle": err.summary(by_b=True)})
+        t.update({"band": o.band, "step": o.step, "schedule": SCHEDULE_NAMES[o.schedule],
+                  "band_fraction": st.band_rays / st.rays, "errors_vs_cpu_oracle": err.summary(by_b=True)})
         leg[name] = t
     out["impact_grid"] = leg
     return out
@@ -548,7 +559,7 @@ def batch_leg(r, args, flush, threads, fp32_peak):
     t.update({"workload": f"256 scenes, sides 64-1024 log-uniform ({rays / 1e6:.1f} M rays), M 0.5-2, r_cam 6-50 M, "
                           "incl 0-90 deg, FoV 20-90 deg, disc 6 M to 12-30 M, per-scene seeded textures",
               "tuned": {"step": tuned.step, "band": tuned.band,
-                        "schedule": "persistent" if tuned.schedule == capi.SCHEDULE_PERSISTENT else "grid",
+                        "schedule": SCHEDULE_NAMES[tuned.schedule],
                         "threads_per_block": tuned.threads_per_block, "refill_threshold": tuned.refill_threshold,
                         "slice_steps": tuned.slice_steps, "block": [tuned.block_x, tuned.block_y],
                         "rays_per_thread": tuned.rays_per_thread,
@@ -649,7 +660,9 @@ def run_ours(args):
     # MIXED launches five kernels per render (band classification, the band
     # list's sort, the FP64 band pass, the FP32 pass it launches from the
     # device, the host's draining FP32 launch), the plain tracer one.
-    tuned_kernels = 5 if tuned.schedule == capi.SCHEDULE_PERSISTENT else 1
+    # MIXED on the persistent or hybrid schedule: classification, sort, FP64
+    # band pass, the FP32 pass it launches, the host's draining launch
+    tuned_kernels = 1 if tuned.schedule == capi.SCHEDULE_GRID else 5
     ms_tuned, st_tuned, wall_tuned = time_steps(tuned, tuned_kernels, graph=True)
     eq = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
     plain_tuned = capi.default_options(precision=capi.PRECISION_FP32, step=tuned.step)
@@ -689,7 +702,7 @@ def run_ours(args):
     issue_frac = fp32_steps * capi.RK4_INSTRUCTIONS_PER_STEP / (ms_tuned * 1e-3) / (fp32_tflops * 1e12 / 2)
     variants["mixed_batched_tuned"] = {
         "call": "bh_sequence_launch", "mrays_per_s": round(value, 3), "ms_per_step": round(ms_tuned, 3), "step": tuned.step,
-        "band": tuned.band, "schedule": "persistent" if tuned.schedule == capi.SCHEDULE_PERSISTENT else "grid",
+        "band": tuned.band, "schedule": SCHEDULE_NAMES[tuned.schedule],
         "threads_per_block": tuned.threads_per_block, "refill_threshold": tuned.refill_threshold,
         "slice_steps": tuned.slice_steps, "block": [tuned.block_x, tuned.block_y],
         "rays_per_thread": tuned.rays_per_thread,
@@ -753,7 +766,7 @@ def run_ours(args):
 
     near_critical = batch = None
     if not args.no_stress:
-        near_critical = near_critical_leg(r, args, flush, threads)
+        near_critical = near_critical_leg(r, args, flush, threads, tuned)
         batch = batch_leg(r, args, flush, threads, fp32_tflops)
 
     cpu = None

@@ -28,7 +28,7 @@ RAYGEN_REF, RAYGEN_PINHOLE = 0, 1
 DISC_MAP_REF_PLANAR, DISC_MAP_POLAR = 0, 1
 FORMAT_BGRA8, FORMAT_BGR8, FORMAT_RGBA8 = 0, 1, 2
 TEXEL_BGR8, TEXEL_RGB8, TEXEL_BGRA8, TEXEL_RGBA8 = 0, 1, 2, 3
-SCHEDULE_GRID, SCHEDULE_PERSISTENT = 0, 1
+SCHEDULE_GRID, SCHEDULE_PERSISTENT, SCHEDULE_HYBRID = 0, 1, 2
 CLASS_MISS, CLASS_HORIZON, CLASS_DISC, CLASS_MAXSTEPS, CLASS_OBJECT = 0, 1, 2, 3, 4
 OBJECT_RECTANGLE, OBJECT_TRIANGLE, OBJECT_PLANE = 1, 2, 3
 MAX_OBJECTS = 64

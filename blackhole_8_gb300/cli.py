@@ -20,7 +20,7 @@ import os
 import time
 
 PRECISIONS = {"fp32": 0, "fp64": 1, "mixed": 2}
-SCHEDULES = {"grid": 0, "persistent": 1}
+SCHEDULES = {"grid": 0, "persistent": 1, "hybrid": 2}
 INTEGRATORS = {"ref": 0, "rk4": 1, "flat": 2, "multi": 3}
 
 
@@ -72,7 +72,9 @@ def main(argv=None) -> int:
     ap.add_argument("--refill", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--band-serial", action="store_true",
-                    help="MIXED + persistent: FP32 pass, then FP64 band pass, both host-launched")
+                    help="MIXED + persistent or hybrid: FP32 pass, then FP64 band pass, both host-launched")
+    ap.add_argument("--block", default="", help="GRID / HYBRID block shape WxH (default 8x16)")
+    ap.add_argument("--rays-per-thread", type=int, default=0, help="GRID / HYBRID block tiles per block")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ppm", default="")
     args = ap.parse_args(argv)
@@ -93,7 +95,9 @@ def main(argv=None) -> int:
                                 schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
                                 band=args.band, setup_band=args.setup_band, slice_steps=args.slice,
                                 refill_threshold=args.refill, threads_per_block=args.threads,
-                                band_serial=int(args.band_serial))
+                                band_serial=int(args.band_serial), rays_per_thread=args.rays_per_thread)
+    if args.block:
+        opts.block_x, opts.block_y = (int(v) for v in args.block.lower().split("x"))
     with Renderer(0) as r:
         cs = r.c_scenes(scenes)
         import torch

@@ -541,6 +541,13 @@ int enqueue_kernels(bh_ctx* ctx, LaunchParams& p, const bh_render_options& o, co
     const bool objects = o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI ||
                          count_objects(scenes, n) > 0;
     BH_CUDA(ctx, bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, st, objects));
+  } else if (o.schedule == BH_SCHEDULE_HYBRID) {
+    std::vector<int32_t> w(n), h(n);
+    for (int i = 0; i < n; ++i) {
+      w[i] = scenes[i].camera.width;
+      h[i] = scenes[i].camera.height;
+    }
+    BH_CUDA(ctx, bhgb::launch_hybrid(p, w.data(), h.data(), o.block_x, o.block_y, o.threads_per_block, st));
   } else {
     int blocks = 0;
     int rc = persistent_blocks(ctx, p, o, &blocks);
@@ -575,7 +582,7 @@ int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
   p.n_scenes = n;
   p.total_rays = total;
   p.counters = ctx->d_counters;
-  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
+  if (bhgb::uses_band_pass(o)) {
     const uint32_t cap = band_capacity_for(total);
     if ((rc = ensure_dev(ctx, ctx->band_list, bhgb::band_words(cap)))) return rc;
     bhgb::carve_band(ctx->band_list.ptr, cap, &p.band_list, &p.band_tmp, &p.band_key);
@@ -913,7 +920,7 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
   p.n_scenes = n;
   p.total_rays = total;
   p.counters = q->d_counters;
-  if (o.schedule == BH_SCHEDULE_PERSISTENT && o.precision == BH_PRECISION_MIXED) {
+  if (bhgb::uses_band_pass(o)) {
     q->band_capacity = band_capacity_for(total);
     e = cudaMalloc(&q->band_list, sizeof(uint32_t) * bhgb::band_words(q->band_capacity));
     if (e != cudaSuccess) return fail(cuda_err(ctx, e, "band list"));
@@ -942,6 +949,13 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
       e = bhgb::launch_grid(p, w.data(), h.data(), o.block_x, o.block_y, cs,
                             o.integrator == BH_INTEGRATOR_FLAT || o.integrator == BH_INTEGRATOR_MULTI ||
                                 q->n_objects_total > 0);
+    } else if (o.schedule == BH_SCHEDULE_HYBRID) {
+      std::vector<int32_t> w(n), h(n);
+      for (int i = 0; i < n; ++i) {
+        w[i] = scenes[i].camera.width;
+        h[i] = scenes[i].camera.height;
+      }
+      e = bhgb::launch_hybrid(p, w.data(), h.data(), o.block_x, o.block_y, o.threads_per_block, cs);
     } else {
       e = bhgb::launch_persistent(p, o.threads_per_block, blocks, cs);
     }
@@ -1213,28 +1227,50 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
   for (double h : {0.1, 0.08, 0.05, 0.04, 0.03, 0.02})
     if (h > base.step) steps.push_back(h);
   steps.push_back(base.step);  // the reference step itself is the last resort
+  auto meets = [&](const bh_render_options& c, bool* ok) -> int {
+    int r = render_sample(ctx, sample, sf, c, &got);
+    if (r) return r;
+    report->candidates++;
+    double d, rr, m;
+    compare_sample(ref, got, &d, &rr, &m);
+    *ok = d <= 0.5 * max_error && m <= 1e-4;
+    if (*ok) {
+      report->max_deflection = d;
+      report->max_radius_error = rr;
+      report->class_mismatch = m;
+    }
+    return BH_OK;
+  };
   bool ok = false;
   for (double h : steps) {
     bh_render_options c = base;
     c.step = h;
     c.format = BH_FORMAT_BGRA8;
-    if ((rc = render_sample(ctx, sample, sf, c, &got))) return rc;
-    report->candidates++;
-    double d, r, m;
-    compare_sample(ref, got, &d, &r, &m);
-    if (d <= 0.5 * max_error && m <= 1e-4) {
+    if ((rc = meets(c, &ok))) return rc;
+    if (ok) {
       chosen.step = h;
       report->step = h;
-      report->max_deflection = d;
-      report->max_radius_error = r;
-      report->class_mismatch = m;
-      ok = true;
       break;
     }
   }
   if (!ok) return set_err(ctx, BH_ERR_UNSUPPORTED, "no candidate step meets the deflection bound");
 
-  // 2) the fastest schedule on the whole batch (pixels only)
+  // 2) the narrowest FP64 band (never below 2e-5 M, where FP32 with the FP64
+  // first integral and the energy projection stays within 2e-5 rad of FP64
+  // on an impact-parameter grid) that keeps the sample within the same bound
+  for (double band : {2e-5, 1e-4}) {
+    if (!(band < base.band)) break;
+    bh_render_options c = chosen;
+    c.band = band;
+    c.format = BH_FORMAT_BGRA8;
+    if ((rc = meets(c, &ok))) return rc;
+    if (ok) {
+      chosen.band = band;
+      break;
+    }
+  }
+
+  // 3) the fastest schedule on the whole batch (pixels only)
   std::vector<bh_frame> bf(static_cast<size_t>(n));
   for (int i = 0; i < n; ++i) {
     bf[i].pixels = mem.get(size_t(scenes[i].camera.width) * scenes[i].camera.height * 4, &e);
@@ -1259,33 +1295,41 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
     }
     return BH_OK;
   };
-  // the persistent schedule: band, block size, refill threshold, slice
-  for (double band : {5e-4, 1e-3})
-    for (int threads : {128, 256})
-      for (int refill : {16, 32})
-        for (int slice : {128, 256, 512}) {
-          bh_render_options c = chosen;
-          c.band = std::max(band, base.band);
-          c.threads_per_block = threads;
-          c.refill_threshold = refill;
-          c.slice_steps = slice;
-          c.format = BH_FORMAT_BGRA8;
-          if ((rc = time_candidate(c))) return rc;
-        }
-  // the grid schedule (band rays traced inline): block shape and rays per
-  // thread
-  static const int kShapes[][2] = {{8, 16}, {16, 8}, {32, 4}, {8, 8}, {16, 16}};
+  // persistent: block size, refill threshold, slice
+  for (int threads : {128, 256})
+    for (int refill : {16, 32})
+      for (int slice : {128, 256, 512}) {
+        bh_render_options c = chosen;
+        c.schedule = BH_SCHEDULE_PERSISTENT;
+        c.threads_per_block = threads;
+        c.refill_threshold = refill;
+        c.slice_steps = slice;
+        c.format = BH_FORMAT_BGRA8;
+        if ((rc = time_candidate(c))) return rc;
+      }
+  // hybrid (grid FP32 pass beside the persistent FP64 band pass) and grid
+  // (band rays inline): block shape and rays per thread
+  static const int kShapes[][2] = {{8, 16}, {8, 8}, {16, 8}, {32, 4}};
   for (const auto& sh : kShapes)
-    for (int rpt : {1, 2, 4}) {
+    for (int rpt : {2, 4, 8}) {
       bh_render_options c = chosen;
-      c.schedule = BH_SCHEDULE_GRID;
-      c.band = std::max(5e-4, base.band);
+      c.schedule = BH_SCHEDULE_HYBRID;
       c.block_x = sh[0];
       c.block_y = sh[1];
       c.rays_per_thread = rpt;
+      c.threads_per_block = 128;
       c.format = BH_FORMAT_BGRA8;
       if ((rc = time_candidate(c))) return rc;
     }
+  for (int rpt : {1, 4}) {
+    bh_render_options c = chosen;
+    c.schedule = BH_SCHEDULE_GRID;
+    c.block_x = 8;
+    c.block_y = 16;
+    c.rays_per_thread = rpt;
+    c.format = BH_FORMAT_BGRA8;
+    if ((rc = time_candidate(c))) return rc;
+  }
   best_o.format = opts->format;
   report->kernel_ms = best;
   *opts = best_o;

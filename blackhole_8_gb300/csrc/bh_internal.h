@@ -180,6 +180,10 @@ struct LaunchParams {
   int32_t band_serial;        // persistent MIXED: 1 = FP32 pass, then FP64 pass, from the host
   int32_t mixed_blocks;       // persistent MIXED: grid of the FP32 pass the FP64 pass launches (0: none)
   int32_t rays_per_thread;    // GRID: consecutive block tiles down the image per block (>= 1)
+  int32_t hybrid;             // HYBRID MIXED: the FP32 pass is grid_kernel with band rays deferred
+  int32_t grid_dim[3];        //   its grid and block (the FP64 pass launches it from the device)
+  int32_t block_dim[2];
+  int32_t drain_only;         //   host launch after the FP64 pass: traces only if the device launch failed
 };
 
 // Bound on how much b / M changes between neighbouring pixels of a row. The
@@ -305,6 +309,14 @@ inline float band_key_scale_for(double eps_lo, double eps_hi) {
   return edge > 0 ? float(1.0 / edge) : 0.f;
 }
 
+// True when a render of these options lists the FP64 band rays and traces
+// them in a persistent pass of their own (MIXED on the PERSISTENT or HYBRID
+// schedule): it needs the band list.
+inline bool uses_band_pass(const bh_render_options& o) {
+  return o.precision == BH_PRECISION_MIXED &&
+         (o.schedule == BH_SCHEDULE_PERSISTENT || o.schedule == BH_SCHEDULE_HYBRID);
+}
+
 // The checks of bh_render_options that need no context, shared by every
 // render entry point (bh_render, bh_render_device, bh_sequence_create,
 // bh_render_noalloc) so that they accept and refuse the same options.
@@ -335,12 +347,12 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
     std::snprintf(msg, len, "unknown format %d", o.format);
     return BH_ERR_INVALID_ARGUMENT;
   }
-  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT) {
+  if (o.schedule != BH_SCHEDULE_GRID && o.schedule != BH_SCHEDULE_PERSISTENT && o.schedule != BH_SCHEDULE_HYBRID) {
     std::snprintf(msg, len, "unknown schedule %d", o.schedule);
     return BH_ERR_INVALID_ARGUMENT;
   }
-  if (o.schedule == BH_SCHEDULE_PERSISTENT && (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
-    return bad(BH_ERR_UNSUPPORTED, "the persistent schedule runs RK4 in FP32 or MIXED precision");
+  if (o.schedule != BH_SCHEDULE_GRID && (o.integrator != BH_INTEGRATOR_RK4 || o.precision == BH_PRECISION_FP64))
+    return bad(BH_ERR_UNSUPPORTED, "the persistent and hybrid schedules run RK4 in FP32 or MIXED precision");
   if (!(o.step > 0 && o.step <= 1.0)) return bad(BH_ERR_INVALID_ARGUMENT, "step must be in (0, 1]");
   if (o.max_steps < 1 || o.max_steps > 100000000)
     return bad(BH_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 1e8]");
@@ -375,6 +387,12 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
 // host-launched FP32 pass that drains what is left of the ray queue
 // (band_serial: the FP32 pass, then the FP64 pass, both from the host).
 cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream);
+// HYBRID: as launch_persistent, with the FP32 pass on the GRID schedule
+// (rays_per_thread block tiles per block, band rays deferred); the host's
+// launch after the FP64 pass traces only if the device-side launch failed.
+// FP32 precision: launch_grid.
+cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h, int block_x,
+                          int block_y, int band_threads, cudaStream_t stream);
 cudaError_t persistent_occupancy(const LaunchParams& p, int threads, int* blocks_per_sm);
 cudaError_t launch_fp32_probe(float* sink, int blocks, int threads, int iters, cudaStream_t stream);
 cudaError_t launch_fp64_probe(double* sink, int blocks, int threads, int iters, cudaStream_t stream);

@@ -294,6 +294,13 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
       h[i] = scenes[i].camera.height;
     }
     e = bhgb::launch_grid(p, w, h, o.block_x, o.block_y, st);
+  } else if (o.schedule == BH_SCHEDULE_HYBRID) {
+    int32_t w[BH_NOALLOC_MAX_SCENES], h[BH_NOALLOC_MAX_SCENES];
+    for (int i = 0; i < n; ++i) {
+      w[i] = scenes[i].camera.width;
+      h[i] = scenes[i].camera.height;
+    }
+    e = bhgb::launch_hybrid(p, w, h, o.block_x, o.block_y, o.threads_per_block, st);
   } else {
     int per_sm = o.blocks_per_sm, sms = 0;
     if (per_sm == 0) {

@@ -98,11 +98,14 @@ enum { BH_FORMAT_BGRA8 = 0, BH_FORMAT_BGR8 = 1, BH_FORMAT_RGBA8 = 2 };
 /* Texture layouts accepted by bh_texture_create. BGR8 is cv::Mat CV_8UC3. */
 enum { BH_TEXEL_BGR8 = 0, BH_TEXEL_RGB8 = 1, BH_TEXEL_BGRA8 = 2, BH_TEXEL_RGBA8 = 3 };
 
-/* Work schedule. GRID: one thread per pixel over a 2-D grid per frame.
+/* Work schedule. GRID: one thread per pixel of rays_per_thread block tiles
+ * over a 2-D grid per frame (MIXED: FP64 band rays traced inline).
  * PERSISTENT: one work-stealing launch over every frame of the call, warps
  * refill finished lanes with new rays; FP64 band rays are deferred to a
- * second persistent pass. */
-enum { BH_SCHEDULE_GRID = 0, BH_SCHEDULE_PERSISTENT = 1 };
+ * second persistent pass. HYBRID (RK4, FP32 or MIXED): MIXED runs the FP32
+ * pass on the GRID schedule with the FP64 band rays deferred to the
+ * persistent FP64 pass, which runs beside it; FP32 is the GRID schedule. */
+enum { BH_SCHEDULE_GRID = 0, BH_SCHEDULE_PERSISTENT = 1, BH_SCHEDULE_HYBRID = 2 };
 
 /* Per-pixel hit classes written to bh_frame.hit_class. OBJECT: one of the
  * scene's bh_objects (aux holds its index). */
@@ -326,10 +329,13 @@ void bh_sequence_destroy(bh_sequence* seq);
  *      whose MIXED render of the sample stays within max_error / 2 rad of the
  *      reference deflection on every escaped ray with an agreeing class, with
  *      classes agreeing on >= 99.99 % of pixels;
- *   3. times the schedule candidates on the whole batch and keeps the
- *      fastest: PERSISTENT with band {5e-4, 1e-3} x threads {128, 256} x
- *      refill {16, 32} x slice {128, 256, 512}, and GRID with block shapes
- *      {8x16, 16x8, 32x4, 8x8, 16x16} x rays per thread {1, 2, 4}.
+ *   3. takes the narrowest FP64 band in {2e-5, 1e-4} (when below the
+ *      options' band) whose MIXED render of the sample meets the same bound;
+ *   4. times the schedule candidates on the whole batch and keeps the
+ *      fastest: PERSISTENT with threads {128, 256} x refill {16, 32} x
+ *      slice {128, 256, 512}; HYBRID with block shapes {8x16, 8x8, 16x8,
+ *      32x4} x rays per thread {2, 4, 8}; GRID 8x16 with rays per thread
+ *      {1, 4}.
  * `opts` is read as the base (integrator must be RK4) and overwritten with
  * the choice (precision MIXED). When cache_path is not
  * NULL the choice is looked up there first (key: device, batch shape,

@@ -105,16 +105,35 @@ def test_rk4_fp32_matches_oracle(renderer, single):
     compare(out, o, boundary_pixels(o, band=0.1), aux_tol=1e-4)
 
 
-@pytest.mark.parametrize("schedule", [capi.SCHEDULE_GRID, capi.SCHEDULE_PERSISTENT])
+@pytest.mark.parametrize("schedule", [capi.SCHEDULE_GRID, capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_HYBRID])
 def test_rk4_mixed_meets_bound_on_every_escaped_ray(renderer, single, schedule):
     sc, o = single
-    out = renderer.render([sc], opts(precision=capi.PRECISION_MIXED, schedule=schedule), hit_class=True,
-                          aux=True)[0]
+    out = renderer.render([sc], opts(precision=capi.PRECISION_MIXED, schedule=schedule, rays_per_thread=4),
+                          hit_class=True, aux=True)[0]
     st = renderer.stats()
     assert st.rays == 320 * 180
     assert st.band_overflow == 0
     # near the critical impact parameter only the class itself may flip
     compare(out, o, boundary_pixels(o, band=1e-4), aux_tol=1e-4)
+
+
+def test_hybrid_matches_persistent(renderer, single):
+    """The hybrid schedule traces every ray with the persistent schedule's
+    per-ray code (FP32 pass on a grid, the same FP64 band pass): the same
+    rays go to the band, and the images agree up to the compiler's
+    multiply-add contraction in the two FP32 kernels."""
+    sc, _ = single
+    a = renderer.render([sc], opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT),
+                        hit_class=True, aux=True)[0]
+    sa = renderer.stats()
+    b = renderer.render([sc], opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_HYBRID, rays_per_thread=4),
+                        hit_class=True, aux=True)[0]
+    sb = renderer.stats()
+    assert (sa.rays, sa.band_rays, sa.band_steps) == (sb.rays, sb.band_rays, sb.band_steps)
+    assert (a.hit_class == b.hit_class).mean() >= 0.9999
+    assert (a.pixels != b.pixels).any(-1).mean() <= 1e-3
+    assert np.quantile(np.abs(a.aux - b.aux), 0.999) <= 1e-5
+    assert abs(int(sa.steps) - int(sb.steps)) <= 1e-4 * sa.steps
 
 
 def test_persistent_matches_grid(renderer, single):
@@ -207,15 +226,17 @@ def test_pinhole_raygen_differs_from_ref(renderer):
 @pytest.mark.parametrize("precision,schedule", [(capi.PRECISION_FP64, capi.SCHEDULE_GRID),
                                                 (capi.PRECISION_FP32, capi.SCHEDULE_GRID),
                                                 (capi.PRECISION_MIXED, capi.SCHEDULE_GRID),
-                                                (capi.PRECISION_MIXED, capi.SCHEDULE_PERSISTENT)],
-                         ids=["fp64", "fp32", "mixed-grid", "mixed-persistent"])
+                                                (capi.PRECISION_MIXED, capi.SCHEDULE_PERSISTENT),
+                                                (capi.PRECISION_MIXED, capi.SCHEDULE_HYBRID)],
+                         ids=["fp64", "fp32", "mixed-grid", "mixed-persistent", "mixed-hybrid"])
 def test_cfg0_full_size(renderer, precision, schedule):
     """The single-scene workload at its own 640x360 against the FP64 oracle,
     every pixel: FP64 to rounding, MIXED within 1e-4 rad on every escaped
     ray, plain FP32 within 1e-4 rad outside |b - b_c| < 0.1 M."""
     sc = S.single_scene(640, 360)
     o = oracle.render_rk4(sc)
-    out = renderer.render([sc], opts(precision=precision, schedule=schedule), hit_class=True, aux=True)[0]
+    out = renderer.render([sc], opts(precision=precision, schedule=schedule, rays_per_thread=4), hit_class=True,
+                          aux=True)[0]
     if precision == capi.PRECISION_FP64:
         compare(out, o, boundary_pixels(o, band=1e-6, tex=1e-6, edge=1e-9), aux_tol=1e-6)
     elif precision == capi.PRECISION_FP32:
@@ -272,8 +293,9 @@ def test_batched_uneven_scenes(renderer):
     assert agree / total >= 0.999
 
 
-@pytest.mark.parametrize("band", [5e-4, 0.05, 0.2])
-def test_mixed_band_order_is_bit_exact(renderer, band):
+@pytest.mark.parametrize("schedule", [capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_HYBRID])
+@pytest.mark.parametrize("band", [2e-5, 5e-4, 0.05, 0.2])
+def test_mixed_band_order_is_bit_exact(renderer, band, schedule):
     """The FP64 band pass beside the FP32 pass (it launches the FP32 pass
     from the device) and the serial order (both passes launched by the host)
     trace every ray with the same code: frames, classes, deflections and
@@ -285,7 +307,7 @@ def test_mixed_band_order_is_bit_exact(renderer, band):
     pixels = sum(s.camera.width() * s.camera.height() for s in scenes)
     res = []
     for serial in (0, 1):
-        o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, band=band, band_serial=serial)
+        o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, band=band, band_serial=serial, rays_per_thread=3)
         res.append((renderer.render(scenes, o, hit_class=True, aux=True), renderer.stats()))
     (a, sa), (b, sb) = res
     for fa, fb in zip(a, b):
@@ -317,10 +339,11 @@ def _device_frames(torch, scenes, with_cls=True):
     return bufs, frames
 
 
-def test_sequence_graph_matches_direct_render(renderer):
+@pytest.mark.parametrize("schedule", [capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_HYBRID])
+def test_sequence_graph_matches_direct_render(renderer, schedule):
     torch = pytest.importorskip("torch")
     scenes = S.flythrough(6, 96, 54)
-    o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT)
+    o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, rays_per_thread=2)
     bufs, frames = _device_frames(torch, scenes)
     seq = renderer.sequence(renderer.c_scenes(scenes), frames, o)
     seq.launch()

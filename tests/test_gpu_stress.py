@@ -38,9 +38,10 @@ def _band_pixels(scene, band):
     return np.concatenate(out)
 
 
-def test_photon_ring_4096(renderer):
+@pytest.mark.parametrize("schedule", [capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_HYBRID])
+def test_photon_ring_4096(renderer, schedule):
     sc = S.photon_ring_scene(4096)
-    o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, max_steps=20000)
+    o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=schedule, max_steps=20000, rays_per_thread=4)
     fb = renderer.render([sc], o, hit_class=True, aux=True)[0]
     st = renderer.stats()
     assert st.rays == 4096 * 4096 and st.flags == 0 and st.band_overflow == 0
@@ -78,9 +79,13 @@ def batch():
     return S.batched_scenes(256)
 
 
-@pytest.mark.parametrize("step", [0.01, 0.1])
-def test_uneven_batch_256(renderer, batch, step):
-    o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT, step=step)
+@pytest.mark.parametrize("step,schedule,band", [(0.01, capi.SCHEDULE_PERSISTENT, 5e-4),
+                                               (0.1, capi.SCHEDULE_PERSISTENT, 5e-4),
+                                               (0.1, capi.SCHEDULE_HYBRID, 2e-5)],
+                         ids=["persistent-0.01", "persistent-0.1", "hybrid-0.1-band2e-5"])
+def test_uneven_batch_256(renderer, batch, step, schedule, band):
+    o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=schedule, step=step, band=band,
+                             rays_per_thread=4)
     out = renderer.render(batch, o, hit_class=True, aux=True)
     st = renderer.stats()
     assert st.rays == sum(s.camera.width() * s.camera.height() for s in batch) and st.flags == 0

@@ -20,9 +20,11 @@ def test_autotune_choice_meets_bound(renderer, tmp_path):
     opts, rep = renderer.autotune(cs, max_error=1e-4, cache_path=cache)
     assert rep.from_cache == 0 and rep.candidates > 2
     assert opts.precision == capi.PRECISION_MIXED
-    assert opts.schedule in (capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_GRID)
-    # 24 persistent and 15 grid schedule candidates after the step candidates
-    assert rep.candidates >= 1 + 24 + 15
+    assert opts.schedule in (capi.SCHEDULE_PERSISTENT, capi.SCHEDULE_GRID, capi.SCHEDULE_HYBRID)
+    assert opts.band in (2e-5, 1e-4, 5e-4)
+    # 12 persistent, 12 hybrid and 2 grid schedule candidates after the step
+    # (and band) candidates
+    assert rep.candidates >= 1 + 12 + 12 + 2
     assert 0.01 <= opts.step <= 0.1
     assert rep.max_deflection <= 5e-5 and rep.class_mismatch <= 1e-4
     # the choice against the FP64 oracle on a seeded pixel sample of two frames

@@ -54,6 +54,8 @@ CASES = [
      capi.FORMAT_BGRA8),
     ("persistent-fp32", capi.SCHEDULE_PERSISTENT, capi.PRECISION_FP32, capi.INTEGRATOR_RK4, capi.RAYGEN_REF,
      capi.FORMAT_BGRA8),
+    ("hybrid-mixed-bgr8", capi.SCHEDULE_HYBRID, capi.PRECISION_MIXED, capi.INTEGRATOR_RK4, capi.RAYGEN_REF,
+     capi.FORMAT_BGR8),
     ("grid-mixed", capi.SCHEDULE_GRID, capi.PRECISION_MIXED, capi.INTEGRATOR_RK4, capi.RAYGEN_REF,
      capi.FORMAT_BGRA8),
     ("grid-fp32", capi.SCHEDULE_GRID, capi.PRECISION_FP32, capi.INTEGRATOR_RK4, capi.RAYGEN_REF, capi.FORMAT_BGRA8),
