@@ -571,6 +571,7 @@ int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
     resolve_scene(ctx, scenes[i], dframes[i], o, total, ctx->h_scenes.ptr + i);
     total += padded_rays(scenes[i].camera);
   }
+  bhgb::assign_grid_blocks(ctx->h_scenes.ptr, n, o.block_x, o.block_y, o.rays_per_thread);
   const int32_t nobj = count_objects(scenes, n);
   if (nobj > 0) {
     if ((rc = ensure_pinned(ctx, ctx->h_objects, nobj))) return rc;
@@ -914,6 +915,7 @@ int bh_sequence_create(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_
     resolve_scene(ctx, scenes[i], frames[i], o, total, q->h_scenes + i);
     total += padded_rays(scenes[i].camera);
   }
+  bhgb::assign_grid_blocks(q->h_scenes, n, o.block_x, o.block_y, o.rays_per_thread);
   if (q->n_objects_total > 0) resolve_objects(ctx, scenes, n, q->h_objects, q->d_objects, q->h_scenes);
   LaunchParams p = base_params(o);
   p.scenes = q->d_scenes;
@@ -998,6 +1000,7 @@ int bh_sequence_update(bh_sequence* q, const bh_scene* scenes, int32_t n) {
     total += padded_rays(scenes[i].camera);
     q->scenes[i] = scenes[i];
   }
+  bhgb::assign_grid_blocks(q->h_scenes, n, q->opts.block_x, q->opts.block_y, q->opts.rays_per_thread);
   if (q->n_objects_total > 0) resolve_objects(ctx, scenes, n, q->h_objects, q->d_objects, q->h_scenes);
   return BH_OK;
 }

@@ -90,6 +90,9 @@ struct DevScene {
   int32_t tiles_x_shift;      // tile / tiles_x == (tile * tiles_x_magic) >> tiles_x_shift
   uint64_t tiles_x_magic;     //   for every tile index below 2^31 (DivMagic)
   int64_t ray_begin;          // first ray index of this scene (persistent)
+  int64_t block_begin;        // GRID / HYBRID: index of this frame's first block (assign_grid_blocks)
+  int32_t blocks_x;           //   blocks per block row of this frame
+  int32_t pad_blocks;
   const DevObject* objects;   // this scene's objects (n_objects of them)
   int32_t n_objects;
   int32_t n_holes;            // MULTI: holes[0] is the scene's hole, then the extra holes
@@ -376,6 +379,29 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
   if (o.rays_per_thread < 0 || o.rays_per_thread > 8)
     return bad(BH_ERR_INVALID_ARGUMENT, "rays_per_thread must be in [0, 8]");
   return BH_OK;
+}
+
+// GRID / HYBRID blocks of a frame: block_x columns by rays_per_thread tiles of
+// block_y rows.
+inline int64_t grid_blocks_x(int w, int bx) { return (int64_t(w) + bx - 1) / bx; }
+inline int64_t grid_blocks_y(int h, int by, int rpt) {
+  const int64_t rows = int64_t(by) * (rpt > 0 ? rpt : 1);
+  return (int64_t(h) + rows - 1) / rows;
+}
+inline int64_t grid_blocks(int w, int h, int bx, int by, int rpt) {
+  return grid_blocks_x(w, bx) * grid_blocks_y(h, by, rpt);
+}
+// Numbers the frames' GRID blocks back to back, so that a launch over frames
+// of uneven sizes has no empty blocks (block_begin, blocks_x of each record);
+// returns the launch's block count, which launch_grid computes the same way.
+inline int64_t assign_grid_blocks(DevScene* d, int n, int bx, int by, int rpt) {
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    d[i].blocks_x = int32_t(grid_blocks_x(d[i].width, bx));
+    d[i].block_begin = total;
+    total += grid_blocks(d[i].width, d[i].height, bx, by, rpt);
+  }
+  return total;
 }
 
 // Launchers (bh_kernels.cu). All enqueue on `stream` and return a cudaError_t.

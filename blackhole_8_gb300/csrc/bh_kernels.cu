@@ -1285,6 +1285,24 @@ __device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, b
          (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
 }
 
+// The frame of this GRID block and the block's column and row of block tiles
+// in it: blocks enumerate the frames' blocks back to back (block_begin), so
+// a binary search over the frames' first blocks finds it (once per block).
+__device__ __forceinline__ int grid_block_frame(const LaunchParams& p, int* bxi, int* byi) {
+  const long long b = blockIdx.x;
+  int lo = 0, hi = p.n_scenes - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p.scenes[mid].block_begin <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const int local = int(b - p.scenes[lo].block_begin);
+  const int bx_count = p.scenes[lo].blocks_x;
+  *byi = local / bx_count;
+  *bxi = local - *byi * bx_count;
+  return lo;
+}
+
 // GRID store of pixel (x, y) (`valid`: it lies in the frame). In BGR8 frames
 // a warp of a block whose rows are whole warps or hold a whole number of
 // warp rows writes packed words. Called by all 32 lanes of the warp.
@@ -1310,12 +1328,13 @@ __device__ __forceinline__ void grid_store(const DevScene& s, int format, int x,
 template <int kPrecision, int kIntegrator, bool kDefer = false>
 __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   if (kDefer && p.drain_only && !(p.counters->flags & kFlagBandLaunchFailed)) return;
-  const DevScene& s = p.scenes[blockIdx.z];
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int bxi, byi;
+  const DevScene& s = p.scenes[grid_block_frame(p, &bxi, &byi)];
+  const int x = bxi * blockDim.x + threadIdx.x;
   // every lane stays to the end: BGR8 stores are whole-warp operations
   unsigned long long steps_all = 0, rays = 0, band_rays = 0, band_steps = 0;
   for (int k = 0; k < p.rays_per_thread; ++k) {
-    const int row0 = (blockIdx.y * p.rays_per_thread + k) * blockDim.y;
+    const int row0 = (byi * p.rays_per_thread + k) * blockDim.y;
     if (row0 >= s.height) break;  // the same for the whole block
     const int y = row0 + threadIdx.y;
     const bool valid = x < s.width && y < s.height;
@@ -1366,12 +1385,13 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
 // kernel over all six variants took 128).
 template <typename R, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
-  const DevScene& s = p.scenes[blockIdx.z];
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int bxi, byi;
+  const DevScene& s = p.scenes[grid_block_frame(p, &bxi, &byi)];
+  const int x = bxi * blockDim.x + threadIdx.x;
   // every lane stays to the end: BGR8 stores are whole-warp operations
   unsigned long long steps_all = 0, rays = 0;
   for (int k = 0; k < p.rays_per_thread; ++k) {
-    const int row0 = (blockIdx.y * p.rays_per_thread + k) * blockDim.y;
+    const int row0 = (byi * p.rays_per_thread + k) * blockDim.y;
     if (row0 >= s.height) break;  // the same for the whole block
     const int y = row0 + threadIdx.y;
     const bool valid = x < s.width && y < s.height;
@@ -1731,14 +1751,12 @@ __global__ void fp64_probe_kernel(double* sink, int iters) {
 // launchers
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
                         int block_x, int block_y, cudaStream_t stream, bool objects) {
-  int max_w = 0, max_h = 0;
-  for (int i = 0; i < p.n_scenes; ++i) {
-    max_w = scene_w[i] > max_w ? scene_w[i] : max_w;
-    max_h = scene_h[i] > max_h ? scene_h[i] : max_h;
-  }
+  // the frames' blocks back to back (the records' block_begin, assign_grid_blocks)
+  int64_t blocks = 0;
+  for (int i = 0; i < p.n_scenes; ++i) blocks += grid_blocks(scene_w[i], scene_h[i], block_x, block_y, p.rays_per_thread);
+  if (blocks < 1 || blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   const dim3 block(block_x, block_y, 1);
-  const int rows = block_y * std::max(1, p.rays_per_thread);  // image rows per block
-  const dim3 grid((max_w + block_x - 1) / block_x, (max_h + rows - 1) / rows, p.n_scenes);
+  const dim3 grid(unsigned(blocks), 1, 1);
   void (*kernel)(LaunchParams);
   const bool fp64 = p.precision == BH_PRECISION_FP64;
   if (!objects) {
@@ -1813,17 +1831,14 @@ cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const i
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  int max_w = 0, max_h = 0;
-  for (int i = 0; i < p.n_scenes; ++i) {
-    max_w = scene_w[i] > max_w ? scene_w[i] : max_w;
-    max_h = scene_h[i] > max_h ? scene_h[i] : max_h;
-  }
+  int64_t blocks = 0;
+  for (int i = 0; i < p.n_scenes; ++i) blocks += grid_blocks(scene_w[i], scene_h[i], block_x, block_y, p.rays_per_thread);
+  if (blocks < 1 || blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   LaunchParams q = p;
-  const int rows = block_y * std::max(1, p.rays_per_thread);
   q.hybrid = 1;
-  q.grid_dim[0] = (max_w + block_x - 1) / block_x;
-  q.grid_dim[1] = (max_h + rows - 1) / rows;
-  q.grid_dim[2] = p.n_scenes;
+  q.grid_dim[0] = int32_t(blocks);
+  q.grid_dim[1] = 1;
+  q.grid_dim[2] = 1;
   q.block_dim[0] = block_x;
   q.block_dim[1] = block_y;
   q.mixed_blocks = p.band_serial ? 0 : 1;  // nonzero: the FP64 pass launches the FP32 pass

@@ -251,6 +251,7 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
     resolve(scenes[i], frames[i], o, textures, begin, &g_host_scenes[i]);
     begin += padded_rays(scenes[i].camera);
   }
+  bhgb::assign_grid_blocks(g_host_scenes, n, o.block_x, o.block_y, o.rays_per_thread);
   // From pageable host memory: returns once the records are staged by the
   // driver, so the static host array may be rewritten by the next call.
   e = cudaMemcpyAsync(base + kScenesOffset, g_host_scenes, sizeof(DevScene) * size_t(n), cudaMemcpyHostToDevice, st);
