@@ -45,6 +45,18 @@ WORKLOAD = "fly-through 120 frames 1920x1080, r 30M->8M spiral, incl 60->89 deg,
 CPU_SAMPLE_FRAMES = list(range(0, FRAMES, 15))  # 8 frames
 MAX_DEFLECTION_ERROR = 1e-4
 SCHEDULE_NAMES = {0: "grid", 1: "persistent", 2: "hybrid"}
+# DRAM bytes the tuned tracer's FP32 pass (hybrid schedule, step 0.1, band
+# 2e-5, 8x16 blocks, 8 rays per thread) moves per 120-frame fly-through:
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size
+# (23.13 MB read, 942.97 MB written: the BGRA8 frames)
+FLYTHROUGH_DRAM_BYTES = 23.13e6 + 942.97e6
+# the same pass under ncu --set full (16 frames): FP32 arithmetic
+# instructions (FFMA + FMUL + FADD lanes per cycle) against the chip's FP32
+# lane-issue peak, and the FMA pipe's busy fraction
+NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.383
+NCU_FMA_PIPE_FRAC = 0.490
+# algorithmic bytes per ray: the 4-byte frame store and one 4-byte texel read
+ALGO_BYTES_PER_RAY = 8
 
 
 def parse():
@@ -787,7 +799,14 @@ def run_ours(args):
             "autotune": {"step": tuned.step, "candidates": rep.candidates, "seconds": round(tune_s, 2)},
             "variants": variants,
             "roofline": {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_tflops, 3),
-                         "unit": "TFLOP/s", "frac": round(achieved / fp32_tflops, 4), "traffic": None,
+                         "unit": "TFLOP/s", "frac": round(achieved / fp32_tflops, 4),
+                         "traffic": FLYTHROUGH_DRAM_BYTES,
+                         "traffic_note": "ncu DRAM bytes of one full-size launch of the FP32 pass (hybrid, the "
+                                         "tuned options); algorithmic bytes 8 per ray",
+                         "hbm_gbs": round(FLYTHROUGH_DRAM_BYTES / (ms_tuned * 1e-3) / 1e9, 1),
+                         "algorithmic_gbs": round(ALGO_BYTES_PER_RAY * rays_step / (ms_tuned * 1e-3) / 1e9, 1),
+                         "ncu_fp32_instruction_issue_frac": NCU_FP32_INSTRUCTION_ISSUE_FRAC,
+                         "ncu_fma_pipe_frac": NCU_FMA_PIPE_FRAC,
                          "fp32_issue_frac": round(issue_frac, 4),
                          "peak_source": "measured in this run: FMA microbenchmark bh_probe_fp32_peak",
                          "flops_per_step": capi.RK4_ALGO_FLOPS_PER_STEP,
