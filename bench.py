@@ -743,7 +743,9 @@ def run_ours(args):
         st_e2e = r.stats()
         e2e = {"value": round(job_throughput(rays_step, world, dt), 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(st_e2e.h2d_bytes), "d2h_bytes_per_step": int(st_e2e.d2h_bytes),
-               "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)", "call": "bh_render"}
+               "ms_per_step": round(dt * 1e3, 3), "format": "BGR8 (CV_8UC3)", "call": "bh_render",
+               "frames_path": "kernels write the pinned host frames directly"
+               if st_e2e.flags & capi.STATS_DIRECT_HOST else "device frames copied back in chunks"}
 
     adjoint = None
     if not args.no_adjoint:

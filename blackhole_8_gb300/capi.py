@@ -158,6 +158,7 @@ SIGNATURES["bh_render_noalloc"] = (C.c_int, [C.c_int, C.POINTER(Scene), C.c_int3
                                              C.c_int32, C.POINTER(Frame), C.POINTER(RenderOptions), C.c_void_p,
                                              C.c_char_p, C.c_int32])
 NOALLOC_MAX_SCENES = 64
+STATS_DIRECT_HOST = 256  # BH_STATS_DIRECT_HOST: bh_render's kernels wrote the frames into host memory
 NOALLOC_MAX_RAYS = 4000000
 
 

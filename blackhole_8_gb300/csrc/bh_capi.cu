@@ -53,6 +53,7 @@ struct DevBuf {
 constexpr int kMaxChunks = 4;
 
 struct bh_ctx {
+  bool direct_host = false;  // the last render wrote its frames into host memory from the kernels
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
@@ -562,6 +563,7 @@ int enqueue_kernels(bh_ctx* ctx, LaunchParams& p, const bh_render_options& o, co
 // the statistics and the start event run on over the whole call.
 int render_on_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* dframes,
                      const bh_render_options& o, cudaStream_t st, bool first = true) {
+  if (first) ctx->direct_host = false;
   int rc = wait_staging(ctx);
   if (rc) return rc;
   if ((rc = ensure_pinned(ctx, ctx->h_scenes, n))) return rc;
@@ -787,12 +789,63 @@ int bh_render_device(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_fr
   return render_on_device(ctx, scenes, n, frames, o, st);
 }
 
+namespace {
+
+// The device address of host memory the device can reach (page-locked and
+// mapped: cudaHostAlloc, cudaMallocHost, cudaHostRegister), or null for
+// anything else (pageable or device memory).
+void* mapped_host_address(void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// bh_render into host frames the kernels can write directly: one render, no
+// copy-back. The GRID and HYBRID schedules store whole warp rows (BGR8:
+// packed words, blocks widened to 32 pixels so that a warp's 96 bytes are
+// one row segment); the persistent schedule's scattered per-pixel stores
+// would cross the host link one pixel at a time, so it keeps the copy-back.
+// Returns 1 (not taken) when a buffer is not mapped host memory.
+int render_direct_to_host(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
+                          const bh_render_options& o) {
+  if (o.schedule == BH_SCHEDULE_PERSISTENT) return 1;
+  std::vector<bh_frame> hf(n);
+  uint64_t bytes = 0;
+  const int bpp = bytes_per_pixel(o.format);
+  for (int i = 0; i < n; ++i) {
+    hf[i].pixels = mapped_host_address(frames[i].pixels);
+    hf[i].hit_class = static_cast<uint8_t*>(mapped_host_address(frames[i].hit_class));
+    hf[i].aux = static_cast<float*>(mapped_host_address(frames[i].aux));
+    if (!hf[i].pixels || (frames[i].hit_class && !hf[i].hit_class) || (frames[i].aux && !hf[i].aux)) return 1;
+    const uint64_t px = uint64_t(scenes[i].camera.width) * scenes[i].camera.height;
+    bytes += px * bpp + (frames[i].hit_class ? px : 0) + (frames[i].aux ? px * sizeof(float) : 0);
+  }
+  bh_render_options od = o;
+  if (od.format == BH_FORMAT_BGR8 && od.block_x < 32) {
+    od.block_y = std::max(1, od.block_x * od.block_y / 32);
+    od.block_x = 32;
+  }
+  int rc = render_on_device(ctx, scenes, n, hf.data(), od, ctx->stream, true);
+  if (rc) return rc;
+  ctx->d2h_bytes = bytes;
+  ctx->direct_host = true;
+  BH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return bh_get_stats(ctx, &ctx->last);
+}
+
+}  // namespace
+
 int bh_render(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
               const bh_render_options* opts) {
   bh_render_options o;
   int rc = check_inputs(ctx, scenes, n, frames, opts, &o);
   if (rc) return rc;
   BH_CUDA(ctx, cudaSetDevice(ctx->device));
+  if ((rc = render_direct_to_host(ctx, scenes, n, frames, o)) != 1) return rc;
   // device arena: pixels | classes | aux for every frame, 256-byte aligned
   const int bpp = bytes_per_pixel(o.format);
   std::vector<bh_frame> dframes(n);
@@ -875,6 +928,7 @@ int bh_get_stats(bh_ctx* ctx, bh_render_stats* out) {
   s.kernel_ms = ms;
   s.h2d_bytes = ctx->h2d_bytes;
   s.d2h_bytes = ctx->d2h_bytes;
+  if (ctx->direct_host) s.flags |= BH_STATS_DIRECT_HOST;
   *out = s;
   ctx->last = s;
   return BH_OK;

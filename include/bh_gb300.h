@@ -255,6 +255,7 @@ typedef struct bh_render_options {
 } bh_render_options;
 
 /* Counters of the most recent render on a context. */
+#define BH_STATS_DIRECT_HOST 256u
 typedef struct bh_render_stats {
   uint64_t rays;          /* pixels traced */
   uint64_t steps;         /* integration steps summed over rays */
@@ -263,9 +264,12 @@ typedef struct bh_render_stats {
   uint64_t band_overflow; /* band rays that found no slot in the band list
                              (0: the list holds one slot per ray) */
   uint64_t flags;         /* device bits (0 = none): 1 = band list full,
-                             2 = MIXED + PERSISTENT: the device-side launch
-                             of the FP32 pass failed and the host's launch
-                             after it traced the bulk (image still complete) */
+                             2 = MIXED + PERSISTENT or HYBRID: the
+                             device-side launch of the FP32 pass failed and
+                             the host's launch after it traced the bulk
+                             (image still complete); host bit
+                             BH_STATS_DIRECT_HOST: bh_render's kernels wrote
+                             the frames into host memory directly */
   double kernel_ms;       /* device time of the launches, CUDA events */
   uint64_t h2d_bytes;     /* bytes copied host -> device by the call */
   uint64_t d2h_bytes;     /* bytes copied device -> host by the call
@@ -295,7 +299,13 @@ int bh_texture_destroy(bh_ctx* ctx, int32_t id);
 /* ---- render ---------------------------------------------------------------
  * Replaces the frame body blackhole_solution_test.cc:161-298 for n scenes.
  * bh_render: host frames; uploads the scenes, renders, copies the frames back
- * and returns when they are in host memory.
+ * and returns when they are in host memory. When every buffer of every frame
+ * is page-locked host memory the device can address (cudaHostAlloc,
+ * cudaMallocHost or cudaHostRegister) and the schedule is GRID or HYBRID,
+ * the kernels write the frames there directly (no device copy, no
+ * copy-back; stats flag BH_STATS_DIRECT_HOST); BGR8 frames are then written
+ * with blocks 32 pixels wide (same threads per block), so that each warp
+ * stores whole 96-byte row segments over the host link.
  * bh_render_device: frames in device memory; enqueued on `stream` (a
  * cudaStream_t, NULL = the context's stream) and returns without waiting. */
 int bh_render(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,

@@ -384,6 +384,43 @@ def test_host_render_in_chunks_matches_device_render(renderer):
         assert np.array_equal(px.cpu().numpy(), h.pixels)
 
 
+@pytest.mark.parametrize("schedule,fmt", [(capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8),
+                                          (capi.SCHEDULE_HYBRID, capi.FORMAT_BGRA8),
+                                          (capi.SCHEDULE_GRID, capi.FORMAT_BGR8),
+                                          (capi.SCHEDULE_PERSISTENT, capi.FORMAT_BGR8)],
+                         ids=["hybrid-bgr8", "hybrid-bgra8", "grid-bgr8", "persistent-bgr8"])
+def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt):
+    """bh_render into page-locked host frames: on the GRID and HYBRID
+    schedules the kernels write them directly (stats flag, no device copy),
+    on the persistent schedule the frames are copied back as for pageable
+    memory; either way the frames, classes and deflections equal those of
+    the render into pageable host memory, and d2h_bytes counts every byte of
+    every buffer."""
+    torch = pytest.importorskip("torch")
+    scenes = S.flythrough(3, 320, 180) + [S.single_scene(200, 117)]
+    o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, format=fmt, rays_per_thread=4)
+    ref = renderer.render(scenes, o, hit_class=True, aux=True)
+    assert not renderer.stats().flags & capi.STATS_DIRECT_HOST
+    bpp = 3 if fmt == capi.FORMAT_BGR8 else 4
+    bufs, frames = [], (capi.Frame * len(scenes))()
+    for i, s in enumerate(scenes):
+        h, w = s.camera.height(), s.camera.width()
+        px = torch.zeros((h, w, bpp), dtype=torch.uint8).pin_memory()
+        cl = torch.zeros((h, w), dtype=torch.uint8).pin_memory()
+        ax = torch.zeros((h, w), dtype=torch.float32).pin_memory()
+        bufs.append((px, cl, ax))
+        frames[i] = capi.Frame(px.data_ptr(), cl.data_ptr(), ax.data_ptr())
+    renderer.render_into(renderer.c_scenes(scenes), frames, o)
+    st = renderer.stats()
+    direct = bool(st.flags & capi.STATS_DIRECT_HOST)
+    assert direct == (schedule != capi.SCHEDULE_PERSISTENT)
+    assert st.d2h_bytes == sum(s.camera.width() * s.camera.height() * (bpp + 1 + 4) for s in scenes)
+    for (px, cl, ax), r in zip(bufs, ref):
+        assert np.array_equal(px.numpy(), r.pixels)
+        assert np.array_equal(cl.numpy(), r.hit_class)
+        assert np.array_equal(ax.numpy().view(np.uint32), r.aux.view(np.uint32))
+
+
 def test_render_device_on_torch_stream(renderer):
     torch = pytest.importorskip("torch")
     scenes = [S.single_scene(64, 36)]
