@@ -555,8 +555,8 @@ class Renderer {
     out = std::move(imgs[0]);
   }
 
-  // Batched: every scene in one call (one persistent launch when
-  // opts.schedule is BH_SCHEDULE_PERSISTENT).
+  // Batched: every scene in one call (one launch over all of them on the
+  // GRID, HYBRID and PERSISTENT schedules).
   template <typename T>
   void Render(const std::vector<Scene<T>>& scenes, std::vector<Image>& out, const Options& opts = Options()) {
     PodTables tables;
