@@ -146,6 +146,11 @@ __device__ __forceinline__ uchar4 texel(const DevTexture& t, long long idx) {
   return __ldg(t.texels + idx);
 }
 
+// Texel (tx, ty) of coordinates already clamped to the texture.
+__device__ __forceinline__ uchar4 texel_at(const DevTexture& t, int tx, int ty) {
+  return __ldg(t.texels + ((long long)ty * t.width + tx));
+}
+
 __device__ __forceinline__ int trunc_to_int(double v) {
   // (int) cast of the reference with out-of-range and NaN values pinned down.
   if (!(v == v)) return 0;
@@ -184,7 +189,7 @@ __device__ uchar4 disc_color_polar(const DevScene& s, V3<R> hit) {
   a -= floor(a);
   int ty = (int)floor(a * R(s.disc_tex.height));
   ty = min(max(ty, 0), s.disc_tex.height - 1);
-  return texel(s.disc_tex, (long long)ty * s.disc_tex.width + tx);
+  return texel_at(s.disc_tex, tx, ty);
 }
 
 template <typename R>
@@ -208,7 +213,7 @@ __device__ uchar4 background_color(const DevScene& s, V3<R> d) {
   tx = tx >= W ? tx - W : (tx < 0 ? 0 : tx);
   int ty = (int)floor(colat * (R(H) / kPi<R>()));
   ty = min(max(ty, 0), H - 1);
-  return texel(s.bg_tex, (long long)ty * W + tx);
+  return texel_at(s.bg_tex, tx, ty);
 }
 
 struct Hit {
@@ -748,9 +753,10 @@ __device__ __noinline__ CrossU crossing_u_fp64(float dcr, int kc, float x, float
 template <typename R, bool kRefine64>
 __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R h) {
   R u = crossing_u<R>(st, h);
-  bool hit = on_disc<R>(s, u);
+  // on_disc, with the crossing radius kept for the refinement test
+  const R rc = shade_div(BH_S(R, s, mass), u);
+  bool hit = u < R(0.5) && rc >= BH_S(R, s, r_in) && rc <= BH_S(R, s, r_out);
   if (kRefine64) {
-    const R rc = shade_div(BH_S(R, s, mass), u);
     const R tol = R(2e-3) * BH_S(R, s, mass);
     if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
       const CrossU r64 = crossing_u_fp64(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
