@@ -143,7 +143,8 @@ def test_noalloc_refuses_several_holes(lib):
 
 
 @pytest.mark.parametrize("bad", [{"band": float("inf")}, {"setup_band": float("inf")}, {"band": float("nan")},
-                                 {"step": 0.0 - 1}, {"slice_steps": 2}, {"block_x": 7, "block_y": 1}])
+                                 {"step": 0.0 - 1}, {"slice_steps": 2}, {"block_x": 7, "block_y": 1},
+                                 {"rays_per_thread": 9}, {"rays_per_thread": -1}, {"schedule": 3}])
 def test_noalloc_refuses_the_options_bh_render_refuses(lib, bad):
     """The option checks are the context entry points' own: non-finite bands
     and out-of-range values are refused with the same status."""
@@ -155,3 +156,18 @@ def test_noalloc_refuses_the_options_bh_render_refuses(lib, bad):
     opts = capi.default_options(**bad)
     rc = lib.bh_render_noalloc(0, cs, 1, textures, 2, frames, C.byref(opts), None, err, len(err))
     assert rc == capi.BH_ERR_INVALID_ARGUMENT, err.value
+
+
+@pytest.mark.parametrize("bad", [{"schedule": capi.SCHEDULE_HYBRID, "precision": capi.PRECISION_FP64},
+                                 {"schedule": capi.SCHEDULE_HYBRID, "integrator": capi.INTEGRATOR_REF_TRAPEZOID}])
+def test_noalloc_refuses_unsupported_schedules(lib, bad):
+    """The hybrid schedule runs the RK4 tracer in FP32 or MIXED: other
+    combinations are refused as unsupported before any device work."""
+    err = C.create_string_buffer(512)
+    sc = S.single_scene(32, 18)
+    ids = {id(sc.disc.texture): 0, id(sc.background): 1}
+    textures, frames = _textures_and_frames(1)
+    cs = (capi.Scene * 1)(sc.to_c(ids))
+    opts = capi.default_options(**bad)
+    rc = lib.bh_render_noalloc(0, cs, 1, textures, 2, frames, C.byref(opts), None, err, len(err))
+    assert rc == capi.BH_ERR_UNSUPPORTED, err.value
