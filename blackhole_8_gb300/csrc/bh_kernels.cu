@@ -1262,17 +1262,26 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
 // word w of a row holds the bytes 4w .. 4w+3 of the row, which come from at
 // most two pixels. Every row must start on a 4-byte boundary (frame base
 // 4-aligned, width and x0 multiples of 4). Called by all 32 lanes.
-__device__ __forceinline__ void store_bgr8_words(uint8_t* frame, int width, int x0, int y0, int bw, uint32_t bgr) {
+template <int kBw>
+__device__ __forceinline__ void store_bgr8_words_w(uint8_t* frame, int width, int x0, int y0, uint32_t bgr) {
+  constexpr int kWpr = 3 * kBw / 4;  // words per row
   const int lane = int(lane_id());
-  const int wpr = (3 * bw) >> 2;  // words per row
-  const int r = lane / wpr, w = lane - r * wpr;
+  const int r = lane / kWpr, w = lane - r * kWpr;  // divisions by constants
   const int k = w % 3;
-  const int src = r * bw + 4 * (w / 3) + k;  // the pixel of the word's first byte
+  const int src = r * kBw + 4 * (w / 3) + k;  // the pixel of the word's first byte
   const uint32_t a = __shfl_sync(kFull, bgr, src & 31);
   const uint32_t b = __shfl_sync(kFull, bgr, (src + 1) & 31);
   if (lane < 24)
     reinterpret_cast<uint32_t*>(frame + 3 * ((long long)(y0 + r) * width + x0))[w] =
         (a >> (8 * k)) | (b << (24 - 8 * k));
+}
+__device__ __forceinline__ void store_bgr8_words(uint8_t* frame, int width, int x0, int y0, int bw, uint32_t bgr) {
+  switch (bw) {  // the same on every lane
+    case 4: store_bgr8_words_w<4>(frame, width, x0, y0, bgr); break;
+    case 8: store_bgr8_words_w<8>(frame, width, x0, y0, bgr); break;
+    case 16: store_bgr8_words_w<16>(frame, width, x0, y0, bgr); break;
+    default: store_bgr8_words_w<32>(frame, width, x0, y0, bgr); break;
+  }
 }
 
 __device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
@@ -1280,13 +1289,13 @@ __device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
 }
 
 // True when the warp's pixels ((x, y) per lane, `valid` where it lies in the
-// frame) form a block of rows of bw pixels starting at lane 0's pixel that
-// store_bgr8_words can write. Called by all 32 lanes; the result is the
-// same on every lane.
+// frame) form a block of rows of bw pixels (a power of two, 4 to 32) starting
+// at lane 0's pixel that store_bgr8_words can write. Called by all 32 lanes;
+// the result is the same on every lane.
 __device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, bool valid, int bw) {
   const int lane = int(lane_id());
   const int x0 = __shfl_sync(kFull, x, 0), y0 = __shfl_sync(kFull, y, 0);
-  const bool mine = valid && x == x0 + lane % bw && y == y0 + lane / bw;
+  const bool mine = valid && x == x0 + (lane & (bw - 1)) && y == y0 + (lane >> (__ffs(bw) - 1));
   return __all_sync(kFull, mine) && (x0 & 3) == 0 && (s.width & 3) == 0 &&
          (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
 }
@@ -1314,8 +1323,11 @@ __device__ __forceinline__ int grid_block_frame(const LaunchParams& p, int* bxi,
 // warp rows writes packed words. Called by all 32 lanes of the warp.
 __device__ __forceinline__ void grid_store(const DevScene& s, int format, int x, int y, bool valid, const Hit& h) {
   if (format == BH_FORMAT_BGR8) {
+    // warps cover whole rows of bw pixels: block rows of a multiple of 32
+    // pixels, or of 4, 8 or 16 (powers of two dividing 32)
     const int bx = int(blockDim.x), bw = bx < 32 ? bx : 32;
-    if ((bx % 32 == 0 || 32 % bx == 0) && (bw & 3) == 0 && bgr8_block_ok(s, x, y, valid, bw)) {
+    const bool rows = (bx & 31) == 0 || (bx >= 4 && bx < 32 && (bx & (bx - 1)) == 0);
+    if (rows && bgr8_block_ok(s, x, y, valid, bw)) {
       store_bgr8_words(s.pixels, s.width, __shfl_sync(kFull, x, 0), __shfl_sync(kFull, y, 0), bw, bgr_word(h));
       store_extras(s, x, y, h);
       return;
