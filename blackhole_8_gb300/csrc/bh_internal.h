@@ -187,6 +187,7 @@ struct LaunchParams {
   int32_t grid_dim[3];        //   its grid and block (the FP64 pass launches it from the device)
   int32_t block_dim[2];
   int32_t drain_only;         //   host launch after the FP64 pass: traces only if the device launch failed
+  int32_t frame_blocks;       // GRID / HYBRID: blocks per frame when every frame has as many (else 0)
 };
 
 // Bound on how much b / M changes between neighbouring pixels of a row. The

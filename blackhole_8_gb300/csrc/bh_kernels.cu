@@ -1306,10 +1306,15 @@ __device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, b
 __device__ __forceinline__ int grid_block_frame(const LaunchParams& p, int* bxi, int* byi) {
   const long long b = blockIdx.x;
   int lo = 0, hi = p.n_scenes - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (p.scenes[mid].block_begin <= b) lo = mid;
-    else hi = mid - 1;
+  if (p.frame_blocks > 0) {
+    // frames of one size: a division instead of a chain of dependent loads
+    lo = int(b / p.frame_blocks);
+  } else {
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.scenes[mid].block_begin <= b) lo = mid;
+      else hi = mid - 1;
+    }
   }
   const int local = int(b - p.scenes[lo].block_begin);
   const int bx_count = p.scenes[lo].blocks_x;
@@ -1767,11 +1772,28 @@ __global__ void fp64_probe_kernel(double* sink, int iters) {
 
 // ---------------------------------------------------------------------------
 // launchers
+// The GRID / HYBRID launch's block count (the frames' blocks back to back, as
+// assign_grid_blocks numbers them) and, when every frame has as many blocks,
+// that number in q.frame_blocks.
+static int64_t frame_block_layout(LaunchParams& q, const int32_t* scene_w, const int32_t* scene_h, int block_x,
+                           int block_y) {
+  int64_t blocks = 0, first = -1;
+  bool uniform = true;
+  for (int i = 0; i < q.n_scenes; ++i) {
+    const int64_t b = grid_blocks(scene_w[i], scene_h[i], block_x, block_y, q.rays_per_thread);
+    if (first < 0) first = b;
+    uniform = uniform && b == first;
+    blocks += b;
+  }
+  q.frame_blocks = uniform && first > 0 && first <= 0x7fffffff ? int32_t(first) : 0;
+  return blocks;
+}
+
 cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h,
                         int block_x, int block_y, cudaStream_t stream, bool objects) {
   // the frames' blocks back to back (the records' block_begin, assign_grid_blocks)
-  int64_t blocks = 0;
-  for (int i = 0; i < p.n_scenes; ++i) blocks += grid_blocks(scene_w[i], scene_h[i], block_x, block_y, p.rays_per_thread);
+  LaunchParams q = p;
+  const int64_t blocks = frame_block_layout(q, scene_w, scene_h, block_x, block_y);
   if (blocks < 1 || blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   const dim3 block(block_x, block_y, 1);
   const dim3 grid(unsigned(blocks), 1, 1);
@@ -1786,7 +1808,7 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
     } else {
       kernel = fp64 ? grid_kernel<BH_PRECISION_FP64, BH_INTEGRATOR_RK4> : grid_kernel<BH_PRECISION_FP32, BH_INTEGRATOR_RK4>;
     }
-    kernel<<<grid, block, 0, stream>>>(p);
+    kernel<<<grid, block, 0, stream>>>(q);
     return cudaGetLastError();
   }
   switch (p.integrator) {
@@ -1804,7 +1826,7 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
       kernel = fp64 ? grid_objects_kernel<double, BH_INTEGRATOR_RK4> : grid_objects_kernel<float, BH_INTEGRATOR_RK4>;
       break;
   }
-  kernel<<<grid, block, 0, stream>>>(p);
+  kernel<<<grid, block, 0, stream>>>(q);
   return cudaGetLastError();
 }
 
@@ -1849,10 +1871,9 @@ cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const i
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  int64_t blocks = 0;
-  for (int i = 0; i < p.n_scenes; ++i) blocks += grid_blocks(scene_w[i], scene_h[i], block_x, block_y, p.rays_per_thread);
-  if (blocks < 1 || blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   LaunchParams q = p;
+  const int64_t blocks = frame_block_layout(q, scene_w, scene_h, block_x, block_y);
+  if (blocks < 1 || blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   q.hybrid = 1;
   q.grid_dim[0] = int32_t(blocks);
   q.grid_dim[1] = 1;
