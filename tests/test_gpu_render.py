@@ -384,21 +384,26 @@ def test_host_render_in_chunks_matches_device_render(renderer):
         assert np.array_equal(px.cpu().numpy(), h.pixels)
 
 
-@pytest.mark.parametrize("schedule,fmt", [(capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8),
-                                          (capi.SCHEDULE_HYBRID, capi.FORMAT_BGRA8),
-                                          (capi.SCHEDULE_GRID, capi.FORMAT_BGR8),
-                                          (capi.SCHEDULE_PERSISTENT, capi.FORMAT_BGR8)],
-                         ids=["hybrid-bgr8", "hybrid-bgra8", "grid-bgr8", "persistent-bgr8"])
-def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt):
+@pytest.mark.parametrize("schedule,fmt,rpt,band", [(capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 4, 5e-4),
+                                                   (capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 8, 0.05),
+                                                   (capi.SCHEDULE_HYBRID, capi.FORMAT_BGRA8, 4, 5e-4),
+                                                   (capi.SCHEDULE_GRID, capi.FORMAT_BGR8, 4, 5e-4),
+                                                   (capi.SCHEDULE_PERSISTENT, capi.FORMAT_BGR8, 1, 5e-4)],
+                         ids=["hybrid-bgr8", "hybrid-bgr8-r8-band0.05", "hybrid-bgra8", "grid-bgr8", "persistent-bgr8"])
+def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt, rpt, band):
     """bh_render into page-locked host frames: on the GRID and HYBRID
-    schedules the kernels write them directly (stats flag, no device copy),
-    on the persistent schedule the frames are copied back as for pageable
-    memory; either way the frames, classes and deflections equal those of
-    the render into pageable host memory, and d2h_bytes counts every byte of
-    every buffer."""
+    schedules the kernels write them directly (stats flag, no device copy;
+    BGR8 rows go out as packed 32-bit words, one 32-pixel row segment per
+    warp), on the persistent schedule the frames are copied
+    back as for pageable memory; either way the frames, classes and
+    deflections equal those of the render into pageable host memory, and
+    d2h_bytes counts every byte of every buffer. Frame widths: multiples of
+    32, of 4 only (block rows partly outside the frame) and of neither
+    (rows not 4-byte aligned: pixel stores); a wide band leaves many tiles
+    with pixels the FP64 pass writes."""
     torch = pytest.importorskip("torch")
-    scenes = S.flythrough(3, 320, 180) + [S.single_scene(200, 117)]
-    o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, format=fmt, rays_per_thread=4)
+    scenes = S.flythrough(3, 320, 180) + [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1]]
+    o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, format=fmt, rays_per_thread=rpt, band=band)
     ref = renderer.render(scenes, o, hit_class=True, aux=True)
     assert not renderer.stats().flags & capi.STATS_DIRECT_HOST
     bpp = 3 if fmt == capi.FORMAT_BGR8 else 4
