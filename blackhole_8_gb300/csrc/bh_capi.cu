@@ -1259,10 +1259,17 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
 
   TuneBuffers mem;
   cudaError_t e = cudaSuccess;
-  // sample: up to 4 scenes, evenly spaced, with class and aux outputs
+  // sample, with class and aux outputs: up to 16 evenly spaced scenes, fewer
+  // (down to 4) while they hold more than eight 1920x1080 frames of pixels
+  auto pick = [n](int k, int i) -> int32_t { return k == 1 ? 0 : int32_t(int64_t(i) * (n - 1) / (k - 1)); };
+  int ns = std::min<int32_t>(n, 16);
+  for (; ns > 4; --ns) {
+    double px = 0;
+    for (int i = 0; i < ns; ++i) px += double(scenes[pick(ns, i)].camera.width) * scenes[pick(ns, i)].camera.height;
+    if (px <= 8.0 * 1920 * 1080) break;
+  }
   std::vector<bh_scene> sample;
-  const int ns = std::min<int32_t>(n, 4);
-  for (int i = 0; i < ns; ++i) sample.push_back(scenes[ns == 1 ? 0 : int64_t(i) * (n - 1) / (ns - 1)]);
+  for (int i = 0; i < ns; ++i) sample.push_back(scenes[pick(ns, i)]);
   std::vector<bh_frame> sf(sample.size());
   for (size_t i = 0; i < sample.size(); ++i) {
     const size_t px = size_t(sample[i].camera.width) * sample[i].camera.height;
@@ -1281,7 +1288,7 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
 
   // 1) the largest step that keeps the sample within max_error / 2
   std::vector<double> steps;
-  for (double h : {0.1, 0.08, 0.05, 0.04, 0.03, 0.02})
+  for (double h : {0.2, 0.175, 0.15, 0.125, 0.1, 0.08, 0.05, 0.04, 0.03, 0.02})
     if (h > base.step) steps.push_back(h);
   steps.push_back(base.step);  // the reference step itself is the last resort
   auto meets = [&](const bh_render_options& c, bool* ok) -> int {

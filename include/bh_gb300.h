@@ -333,12 +333,13 @@ void bh_sequence_destroy(bh_sequence* seq);
  * tracer's RK4 step, FP64 band width, schedule and its shape (persistent:
  * block size, refill threshold, slice length; grid: block shape and rays per
  * thread) for a batch of scenes:
- *   1. renders a sample of the scenes (up to 4, evenly spaced) in FP64 with
- *      the options' step as the reference (the oracle's scheme);
- *   2. takes the largest step in {0.1, 0.08, 0.05, 0.04, 0.03, 0.02, 0.01}
- *      whose MIXED render of the sample stays within max_error / 2 rad of the
- *      reference deflection on every escaped ray with an agreeing class, with
- *      classes agreeing on >= 99.99 % of pixels;
+ *   1. renders a sample of the scenes (up to 16, evenly spaced, fewer while
+ *      they hold more than eight 1920x1080 frames of pixels; at least 4) in
+ *      FP64 with the options' step as the reference (the oracle's scheme);
+ *   2. takes the largest step in {0.2, 0.175, 0.15, 0.125, 0.1, 0.08, 0.05,
+ *      0.04, 0.03, 0.02, 0.01} whose MIXED render of the sample stays within
+ *      max_error / 2 rad of the reference deflection on every escaped ray
+ *      with an agreeing class, with classes agreeing on >= 99.99 % of pixels;
  *   3. takes the narrowest FP64 band in {2e-5, 1e-4} (when below the
  *      options' band) whose MIXED render of the sample meets the same bound;
  *   4. times the schedule candidates on the whole batch and keeps the
