@@ -23,7 +23,9 @@
 // calls. Make that first call during set-up, before any stream capture. The
 // kept address is no longer valid after cudaDeviceReset on that device.
 // Each call stages its scene records from a static host array into the device
-// array with cudaMemcpyAsync. All calls share the array and it keeps the last
+// array with cudaMemcpyAsync; a call on a stream that is capturing is refused
+// (BH_ERR_UNSUPPORTED), since the recorded copy would read that host array
+// after later calls rewrote it. All calls share the array and it keeps the last
 // call's contents: the counters are cleared on the caller's stream at the
 // start of each call, and two calls whose work overlaps on the GPU
 // (different streams, or the same stream from different host threads
@@ -236,6 +238,18 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
   std::lock_guard<std::mutex> lock(g_mutex);
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return fail(error, error_len, BH_ERR_NO_DEVICE, "cudaSetDevice: %s", cudaGetErrorString(e));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  {
+    // A captured call would record a copy from g_host_scenes, which the next
+    // call rewrites before the graph replays: refused before any device work.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess)
+      return fail(error, error_len, BH_ERR_CUDA, "cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail(error, error_len, BH_ERR_UNSUPPORTED,
+                  "the stream is capturing: a call stages its scenes from a host array that the next call rewrites");
+  }
   if (!g_scratch_ptr[device]) {  // once per device, with that device current
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_scratch);
@@ -244,7 +258,6 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
     g_scratch_ptr[device] = static_cast<unsigned char*>(ptr);
   }
   unsigned char* base = g_scratch_ptr[device];
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   int64_t begin = 0;
   for (int i = 0; i < n; ++i) {

@@ -382,7 +382,9 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
  * array's address: make that first call during set-up, before any stream
  * capture. The address is kept for later calls and is no longer valid after
  * cudaDeviceReset. Each call copies its scene records from a static host
- * array with cudaMemcpyAsync. All calls share the array: calls whose work
+ * array with cudaMemcpyAsync; a call on a stream that is capturing is refused
+ * with BH_ERR_UNSUPPORTED (the recorded copy would read that host array after
+ * later calls rewrote it). All calls share the array: calls whose work
  * overlaps on the GPU race. Enqueued on `stream`
  * (a cudaStream_t, NULL = the legacy default stream); returns without
  * waiting. `error` (may be NULL) receives a message of at most error_len

@@ -102,6 +102,39 @@ def test_noalloc_matches_context_entry_point(renderer, case):
                 assert np.abs(ax.cpu().numpy() - r.aux).max() <= 1e-6
 
 
+@pytest.mark.gpu
+def test_noalloc_refuses_a_capturing_stream():
+    """A call made while its stream captures a CUDA graph is refused before
+    any device work: the copy it would record reads the entry point's static
+    host array of scene records, which later calls rewrite before a replay."""
+    torch = pytest.importorskip("torch")
+    lib = capi.load()
+    disc_tex, sky = S.standard_textures(0)
+    tex_bufs, textures = _device_textures(torch, [disc_tex, sky])
+    scenes = [S.single_scene(64, 36)]
+    ids = {id(disc_tex): 0, id(sky): 1}
+    cs = (capi.Scene * 1)(*[s.to_c(ids) for s in scenes])
+    bufs, frames = _device_frames(torch, scenes, 4, with_aux=False)
+    torch.cuda.synchronize()
+    err = C.create_string_buffer(512)
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        graph.capture_begin()
+        try:
+            rc = lib.bh_render_noalloc(0, cs, 1, textures, len(tex_bufs), frames, None, side.cuda_stream, err,
+                                       len(err))
+        finally:
+            graph.capture_end()
+    assert rc == capi.BH_ERR_UNSUPPORTED, err.value
+    assert b"capturing" in err.value
+    # the refusal left the stream and the entry point usable
+    rc = lib.bh_render_noalloc(0, cs, 1, textures, len(tex_bufs), frames, None, None, err, len(err))
+    assert rc == capi.BH_OK, err.value.decode()
+    torch.cuda.synchronize()
+    assert int(bufs[0][1].max().item()) > 0  # classes were written
+
+
 def _textures_and_frames(n):
     # placeholders: these calls are refused before any pointer is used
     textures = (capi.DeviceTexture * 2)(capi.DeviceTexture(1, 1024, 64), capi.DeviceTexture(1, 2048, 1024))
