@@ -42,6 +42,7 @@
 
 #include <cmath>
 
+#include "bh_df.cuh"
 #include "bh_internal.h"
 
 #if defined(__CUDACC__)
@@ -952,62 +953,9 @@ BHA_HD void backward(const AdjScene& s, const AdjParams& p, const RayC<R, P>& rc
 // Backward pass over states stored by forward<..., kStore>, in precision R.
 // p must describe the stored trajectory: for R = float the FP64 step in c32
 // (rounded), inv_h32 and hstep32 (band_view).
-// ---------------------------------------------------------------------------
-// double-float arithmetic (an unevaluated sum hi + lo of two floats, ~48
-// significant bits) by the error-free transformations of Knuth (2Sum) and
-// Dekker (Fast2Sum), with FMA for the exact product error. It runs on the
-// FP32 pipe: on this part an FP64 instruction costs ~80 issue cycles, so a
-// serial FP64 chain is ~5x slower than the same chain in double-float.
-// The error-free transformations need every sum and product rounded on its
-// own: on the device they use the intrinsics the compiler never fuses into an
-// FMA (it would otherwise contract a product into the following sum across
-// inlined calls, and the error terms would be wrong).
-#if defined(__CUDA_ARCH__)
-#define BHA_FADD(a, b) __fadd_rn((a), (b))
-#define BHA_FSUB(a, b) __fsub_rn((a), (b))
-#define BHA_FMUL(a, b) __fmul_rn((a), (b))
-#else
-// host: a rounded store that no compiler fuses
-inline float bha_round(volatile float v) { return v; }
-#define BHA_FADD(a, b) bha_round((a) + (b))
-#define BHA_FSUB(a, b) bha_round((a) - (b))
-#define BHA_FMUL(a, b) bha_round((a) * (b))
-#endif
-struct DF {
-  float hi, lo;
-};
-BHA_HD DF df_fast2sum(float a, float b) {
-  const float s = BHA_FADD(a, b);
-  return DF{s, BHA_FSUB(b, BHA_FSUB(s, a))};
-}
-BHA_HD DF df_add(DF a, DF b) {
-  const float s = BHA_FADD(a.hi, b.hi);
-  const float bb = BHA_FSUB(s, a.hi);
-  const float e = BHA_FADD(BHA_FSUB(a.hi, BHA_FSUB(s, bb)), BHA_FSUB(b.hi, bb));
-  return df_fast2sum(s, BHA_FADD(e, BHA_FADD(a.lo, b.lo)));
-}
-BHA_HD DF df_mul(DF a, DF b) {
-  const float p = BHA_FMUL(a.hi, b.hi);
-  const float e = fmaf(a.hi, b.hi, -p);
-  return df_fast2sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
-}
-BHA_HD DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
-BHA_HD DF df_mul_f(DF a, float b) {
-  const float p = BHA_FMUL(a.hi, b);
-  const float e = fmaf(a.hi, b, -p);
-  return df_fast2sum(p, fmaf(a.lo, b, e));
-}
-BHA_HD DF df_from(double v) {
-  const float h = float(v);
-  return DF{h, float(v - double(h))};
-}
-BHA_HD double df_to(DF a) { return double(a.hi) + double(a.lo); }
-// a <= b and a < b, exactly
-BHA_HD bool df_le(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
-BHA_HD bool df_lt(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+// double-float arithmetic: DF, df_add, df_mul, ... (bh_df.cuh)
 
-// x (3x + 1)
-BHA_HD DF df_fx(DF x) { return df_mul(x, df_add(df_mul_f(x, 3.0f), DF{1.0f, 0.0f})); }
+// x (3x + 1): df_fx (bh_df.cuh)
 
 // The RK4 step of step() in double-float.
 BHA_HD void df_step(DF& x, DF& w, const float* k) {

@@ -407,6 +407,7 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->inv_mass_f = float(1.0 / d->mass);
   d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
   bhgb::resolve_rk4_constants(d->Fhat, d->Fhat_f, &d->Flen, &d->Flen_f, &d->x0, &d->x0_f, d->F, d->mass);
+  bhgb::resolve_derived(d);
   {
     double pos[BH_MAX_HOLES][3], mass[BH_MAX_HOLES], cen[3], mtot;
     d->n_holes = scene_holes(s, pos, mass, cen, &mtot);
@@ -498,16 +499,10 @@ LaunchParams base_params(const bh_render_options& o) {
   p.c32 = bhgb::make_rk4_consts<float>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.cband = bhgb::make_rk4_consts<double>(o.band_step, 1.0 / o.r_escape, o.max_steps);
+  bhgb::split_band_consts(p.cband, p.band_df);
   p.setup_band = bhgb::setup_band_for(o.band, o.setup_band);
   p.class_band = bhgb::class_band_for(o.band);
-  {
-    const double bc = 3.0 * std::sqrt(3.0);
-    const double lo = bc + o.band, hi = bc - o.band;
-    p.eps_band_lo = 1.0 / (lo * lo) - 1.0 / 27.0;
-    p.eps_band_hi = hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300;
-    if (o.band == 0) p.eps_band_lo = p.eps_band_hi = 0.0;  // empty band
-    p.band_key_scale = bhgb::band_key_scale_for(p.eps_band_lo, p.eps_band_hi);
-  }
+  bhgb::set_band_eps(o.band, &p.eps_band_lo, &p.eps_band_hi, &p.band_key_scale, p.eps_band_df);
   p.refill_threshold = o.refill_threshold;
   p.slice_steps = o.slice_steps;
   p.band_lanes = o.band_lanes;

@@ -81,6 +81,16 @@ struct DevScene {
   float inv_mass_f;
   float Fhat_f[3], Flen_f, x0_f;
   float b_lip;                // bound on |b(x+1) - b(x)| / M along an image row (row_b_lipschitz)
+  // MIXED, double-float (hi, lo) copies for the FP32 passes' rare exact paths:
+  // |e|^2 and |F x e|^2 as quadratic forms in the pixel offsets (a, c), six
+  // coefficients each (resolve_derived), M^2, and M, r_in, r_out for the
+  // crossing refinement
+  float eq_e[6][2], eq_g[6][2], m2_df[2];
+  float mass_df[2], r_in_df[2], r_out_df[2];
+  // FP32 polar disc lookup of a disc centred on the hole (resolve_derived)
+  int32_t disc_centred;       // 1 when the disc centre is the hole's position
+  float disc_tx_scale_f;      // disc texture width / (r_out - r_in)
+  float de1F_f, de2F_f;       // e1 . F^, e2 . F^
 
   DevTexture disc_tex;
   DevTexture bg_tex;
@@ -165,11 +175,13 @@ struct LaunchParams {
   Rk4Consts<float> c32;       // bulk step, FP32
   Rk4Consts<double> c64;      // bulk step, FP64
   Rk4Consts<double> cband;    // band step, FP64 (MIXED)
+  float band_df[8][2];        // cband's h, h/2, h^2/4, h^2/2, h^2/6, h/6, x_esc, x_hor in double-float
   float setup_band;           // |b - b_c| / M below which MIXED takes eps from FP64
   float class_band;           // persistent MIXED: |b - b_c| / M (FP32 b) below which the
                               //   classification takes the FP64 band test (class_band_for)
   double eps_band_lo;         // the FP64 band in terms of eps = 1/(b/M)^2 - 1/27:
   double eps_band_hi;         //   eps(b_c + band) < eps < eps(b_c - band)
+  float eps_band_df[4];       //   the same bounds in double-float: lo (hi, lo), hi (hi, lo)
   int64_t total_rays;         // persistent: sum of padded scene ray counts
   DevCounters* counters;
   uint32_t* band_list;        // persistent MIXED: band rays, longest first (sorted by |eps|)
@@ -239,6 +251,66 @@ inline void resolve_rk4_constants(double* Fhat, float* Fhat_f, double* Flen, flo
   *Flen_f = float(L);
   *x0 = L > 0 ? mass / L - 1.0 / 3.0 : 0.0;
   *x0_f = float(*x0);
+}
+
+// (hi, lo) float split of v: hi = v rounded to float, lo = the rest rounded
+inline void split_df(double v, float* out) {
+  out[0] = float(v);
+  out[1] = float(v - double(out[0]));
+}
+
+// Per-scene values derived from a resolved scene (mass, radii, disc basis,
+// textures, camera vectors and RK4 constants set): the double-float copies
+// and the FP32 polar disc lookup's constants. With the pixel offsets a = W/2 - x, c = H/2 - y, the ray direction is
+// e = E0 + a vy + c vz, so |e|^2 and |F x e|^2 = |G0 + a G1 + c G2|^2 (Gi = F x
+// E0, F x vy, F x vz) are quadratic forms in (a, c); their coefficients, in
+// the order of Q = k0 + a (k1 + a k3) + c (k2 + a k4 + c k5), are formed here
+// in FP64 and split. The mixed tracer's first integral of a near-critical ray
+// is then M^2 |e|^2 / |F x e|^2 - 1/27 in double-float.
+inline void resolve_derived(DevScene* d) {
+  auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+  auto cross = [](const double* u, const double* v, double* o) {
+    o[0] = u[1] * v[2] - u[2] * v[1];
+    o[1] = u[2] * v[0] - u[0] * v[2];
+    o[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  auto form = [&](const double* v0, const double* v1, const double* v2, float (*k)[2]) {
+    const double c[6] = {dot(v0, v0), 2 * dot(v0, v1), 2 * dot(v0, v2), dot(v1, v1), 2 * dot(v1, v2), dot(v2, v2)};
+    for (int i = 0; i < 6; ++i) split_df(c[i], k[i]);
+  };
+  form(d->E0, d->vy, d->vz, d->eq_e);
+  double g0[3], g1[3], g2[3];
+  cross(d->F, d->E0, g0);
+  cross(d->F, d->vy, g1);
+  cross(d->F, d->vz, g2);
+  form(g0, g1, g2, d->eq_g);
+  split_df(d->mass * d->mass, d->m2_df);
+  split_df(d->mass, d->mass_df);
+  split_df(d->r_in, d->r_in_df);
+  split_df(d->r_out, d->r_out_df);
+  d->disc_centred = d->dc[0] == 0 && d->dc[1] == 0 && d->dc[2] == 0 ? 1 : 0;
+  d->disc_tx_scale_f = d->r_out > d->r_in ? float(d->disc_tex.width / (d->r_out - d->r_in)) : 0.f;
+  d->de1F_f = float(dot(d->de1, d->Fhat));
+  d->de2F_f = float(dot(d->de2, d->Fhat));
+}
+
+// The band step's constants in double-float (the band pass integrates in
+// double-float on the FP32 pipe).
+inline void split_band_consts(const Rk4Consts<double>& c, float (*out)[2]) {
+  const double v[8] = {c.h, c.hh, c.q, c.q2, c.h26, c.h6, c.x_esc, c.x_hor};
+  for (int i = 0; i < 8; ++i) split_df(v[i], out[i]);
+}
+
+// The FP64 band of the mixed tracer in terms of eps (empty for band 0), with
+// the sort-key scale and the double-float copies of the bounds.
+inline void set_band_eps(double band, double* eps_lo, double* eps_hi, float* key_scale, float eps_df[4]) {
+  const double bc = 3.0 * std::sqrt(3.0), lo = bc + band, hi = bc - band;
+  *eps_lo = band == 0 ? 0.0 : 1.0 / (lo * lo) - 1.0 / 27.0;
+  *eps_hi = band == 0 ? 0.0 : (hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300);
+  const double edge = std::fmax(std::fabs(*eps_lo), std::fabs(*eps_hi));
+  *key_scale = edge > 0 ? float(1.0 / edge) : 0.f;
+  split_df(*eps_lo, eps_df);
+  split_df(std::fmin(*eps_hi, 1e30), eps_df + 2);  // beyond every eps when b_c - band <= 0
 }
 
 inline void resolve_object(const bh_object& b, const double h[3], DevTexture tex, DevObject* d) {

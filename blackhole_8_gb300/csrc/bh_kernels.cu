@@ -22,11 +22,14 @@
 // eps = w^2 - x^2 - 2 x^3 (= 1/b^2 - 1/27, the G of blackhole_solution.h:
 // 27-29) only to FP32 rounding, and near x = 0 (the saddle of the photon
 // orbit) that drift is amplified by 1/|b - b_c|. The mixed tracer therefore
-// (a) takes b, eps and the plane basis from FP64 ray setup for rays with
-// |b - b_c| < setup_band, (b) projects (x, w) back onto eps = const after
-// every 4-step block spent near the saddle (|x| < 0.1), (c) traces rays with
+// (a) takes eps exactly (double-float, from the per-scene quadratic forms of
+// |e|^2 and |F x e|^2) for rays with |b - b_c| < setup_band, (b) projects
+// (x, w) back onto eps = const after every 4-step block spent near the saddle
+// (|x| < 0.1) by rays with |b - b_c| < 0.3 M, (c) traces rays with
 // |b - b_c| < band fully in FP64 with the band step, and (d) refines
-// disc-plane crossings in FP64.
+// disc-plane crossings near the disc edges in double-float. Double-float
+// (bh_df.cuh) runs on the FP32 pipe, where an FP64 instruction costs a warp
+// ~64-80 issue cycles.
 //
 // The path has no dense contraction, so there is no tensor-core work; it is
 // bound by FP32 issue. Textures (a few MB) stay in L2 and are read once per
@@ -37,6 +40,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "bh_df.cuh"
 #include "bh_internal.h"
 
 namespace bhgb {
@@ -189,6 +193,25 @@ __device__ uchar4 disc_color_polar(const DevScene& s, V3<R> hit) {
   a -= floor(a);
   int ty = (int)floor(a * R(s.disc_tex.height));
   ty = min(max(ty, 0), s.disc_tex.height - 1);
+  return texel_at(s.disc_tex, tx, ty);
+}
+
+// disc_color_polar in FP32 for a disc centred on the hole (the RK4 tracer's
+// crossings lie in its plane): the hit is rw (cos phi F^ + sin phi xv) from
+// the centre, so its radius is rw itself and its azimuth about e1 is
+// atan2(e2 . dir, e1 . dir) of the unit direction, with e1 . F^ and e2 . F^
+// per-scene constants; the texel column scale W / (r_out - r_in) is one too.
+__device__ __forceinline__ uchar4 disc_color_polar_centred(const DevScene& s, float rw, float cp, float sp,
+                                                           V3<float> xv) {
+  const int W = s.disc_tex.width, H = s.disc_tex.height;
+  int tx = (int)floorf((rw - s.r_in_f) * s.disc_tx_scale_f);
+  tx = min(max(tx, 0), W - 1);
+  const float y = fmaf(cp, s.de2F_f, sp * dot(BH_V(float, s, de2), xv));
+  const float x = fmaf(cp, s.de1F_f, sp * dot(BH_V(float, s, de1), xv));
+  float a = atan2_poly(y, x) * 0.159154943f;  // 1 / (2 pi)
+  a -= floorf(a);
+  int ty = (int)floorf(a * float(H));
+  ty = min(max(ty, 0), H - 1);
   return texel_at(s.disc_tex, tx, ty);
 }
 
@@ -663,6 +686,7 @@ struct RayState {
   R ev;         // event payload: u at the disc crossing
   int k, kc;    // steps taken, step index holding the next crossing
   int status;
+  bool near;    // mixed FP32 pass: |b - b_c| < kProjectBand M, (x, w) kept on eps
   V3<R> xv;     // with the scene's F / |F|, the ray's orbital basis rotated to the
                 // camera: position = r (cos(phi - phi0) F^ + sin(phi - phi0) xv)
 };
@@ -684,6 +708,7 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
   const R M = BH_S(R, s, mass);
   st.k = 0;
   st.kc = 0x7fffffff;
+  st.near = false;
   st.dcr = R(0);
   st.ev = R(0);
   const R bm = ray.b * inv_mass<R>(s);
@@ -733,19 +758,28 @@ __device__ __forceinline__ bool on_disc(const DevScene& s, RC u) {
   return rc >= BH_S(RC, s, r_in) && rc <= BH_S(RC, s, r_out);
 }
 
-// FP64 root refinement of an FP32 crossing whose radius lies within 2e-3 M of
-// a disc edge (out of line). The state comes by value: a reference would pin
-// the caller's ray state to its stack frame for the whole step loop.
+// Root refinement of an FP32 crossing whose radius lies within 2e-3 M of a
+// disc edge, in double-float (out of line): the partial step of length
+// dcr - kc h from the step's FP32 start state, and the in/out decision
+// r_in <= M / u <= r_out taken as r_in u <= M <= r_out u (u > 0), without a
+// division. The state comes by value: a reference would pin the caller's ray
+// state to its stack frame for the whole step loop.
 struct CrossU {
   float u;
   int hit;
 };
-__device__ __noinline__ CrossU crossing_u_fp64(float dcr, int kc, float x, float w, float h, const DevScene& s) {
-  const double sc = double(dcr) - double(kc) * double(h);
-  double xd = x, wd = w;
-  rk4_partial<double>(xd, wd, sc);
-  const double u = xd + 1.0 / 3.0;
-  return CrossU{float(u), on_disc<double>(s, u) ? 1 : 0};
+__device__ __noinline__ CrossU crossing_u_df(float dcr, int kc, float x, float w, float h, const DevScene& s) {
+  const float kh = __fmul_rn(float(kc), h);  // kc h exactly, as kh + its rounding error
+  const DF sc = df_sub(df_two_sum(dcr, -kh), DF{fmaf(float(kc), h, -kh), 0.f});
+  DF k[6];
+  df_rk4_consts(sc, k);
+  DF xd{x, 0.f}, wd{w, 0.f};
+  df_rk4_step(xd, wd, k);
+  const DF u = df_add(xd, DF{0x1.555556p-2f, -0x1.555556p-27f});  // + 1/3
+  const DF M{s.mass_df[0], s.mass_df[1]};
+  const bool hit = u.hi > 0.f && u.hi < 0.5f && df_le(df_mul(DF{s.r_in_df[0], s.r_in_df[1]}, u), M) &&
+                   df_le(M, df_mul(DF{s.r_out_df[0], s.r_out_df[1]}, u));
+  return CrossU{u.hi, hit ? 1 : 0};
 }
 
 // Disc-plane crossing inside step kc. kRefine64: FP32 crossing with FP64
@@ -759,7 +793,7 @@ __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R
   if (kRefine64) {
     const R tol = R(2e-3) * BH_S(R, s, mass);
     if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
-      const CrossU r64 = crossing_u_fp64(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
+      const CrossU r64 = crossing_u_df(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
       u = R(r64.u);
       hit = r64.hit != 0;
     }
@@ -813,7 +847,7 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
       }
       k += 4;
       if (kProject) {
-        if (fabs(x) < R(0.1)) project_energy(x, w, st.eps);
+        if (st.near && fabs(x) < R(0.1)) project_energy(x, w, st.eps);
       }
     }
     // single steps up to kstop or the event
@@ -840,6 +874,36 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
   return taken;
 }
 
+// Escape point of an FP32 ray that leaves outward through the whole last
+// step: on the orbit, w^2 = P(x) = eps + x^2 (1 + 2x), so the angle from the
+// step's start (x_a) to x_esc is the orbit integral
+//   dphi = integral over [x_esc, x_a] of dx / sqrt(P(x)),
+// taken by two-point Gauss-Legendre, and w there is -sqrt(P(x_esc)). Against
+// the exact integral from the same x_a at step 0.15 this errs <= 1e-6 rad for
+// cameras within 50 M (the Hermite interpolation below: up to 1e-5 rad). It
+// is used where P varies by less than 30 % over the interval (P decreases
+// with x there, so P(x_a) > 0.7 P(x_esc) bounds every node); otherwise (the
+// ray turned within the step, or a camera close to the escape radius) the
+// caller interpolates. FP64 rays always interpolate.
+template <typename R>
+__device__ __forceinline__ bool escape_by_integral(const RayState<R>& st, const Rk4Consts<R>& c, R* phie, R* we) {
+  if constexpr (sizeof(R) != 4) {
+    return false;
+  } else {
+    const float xa = st.xa, xe = c.x_esc, eps = st.eps;
+    const float Pa = fmaf(xa * xa, fmaf(2.f, xa, 1.f), eps);
+    const float Pe = fmaf(xe * xe, fmaf(2.f, xe, 1.f), eps);
+    if (!(st.wa < 0.f && Pa > 0.f && Pa > 0.7f * Pe)) return false;
+    const float m = 0.5f * (xa + xe), r = 0.5f * (xa - xe);
+    const float x1 = fmaf(-0.57735027f, r, m), x2 = fmaf(0.57735027f, r, m);
+    const float P1 = fmaf(x1 * x1, fmaf(2.f, x1, 1.f), eps);
+    const float P2 = fmaf(x2 * x2, fmaf(2.f, x2, 1.f), eps);
+    *phie = fmaf(r, rsqrtf(P1) + rsqrtf(P2), float(st.k - 1) * c.h);
+    *we = -Pe * rsqrtf(Pe);
+    return true;
+  }
+}
+
 // Shades a finished RK4 ray.
 template <typename R>
 __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c) {
@@ -851,29 +915,36 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     const R rw = shade_div(BH_S(R, s, mass), st.ev);
     R sp, cp;
     shade_sincos(phic, &sp, &cp);
-    const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
     hit.cls = BH_CLASS_DISC;
     if (s.aux) hit.aux = float(R(1) / st.ev);
-    hit.bgra = disc_color(s, p);
+    if (sizeof(R) == 4 && s.disc_map == BH_DISC_MAP_POLAR && s.disc_centred) {
+      hit.bgra = disc_color_polar_centred(s, float(rw), float(cp), float(sp), cast3<float>(st.xv));
+    } else {
+      const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
+      hit.bgra = disc_color(s, p);
+    }
   } else if (st.status == kEscape) {
-    // Cubic Hermite through (xa, wa) and (x, w) over the last step; Newton
-    // for the parameter t where x(t) = x_esc.
-    const R xa = st.xa, xb = st.x, ha = c.h * st.wa, hb = c.h * st.w, xe = c.x_esc;
-    R t = shade_div(xa - xe, xa - xb);
-    t = fmin(fmax(t, R(0)), R(1));
-    for (int i = 0; i < (sizeof(R) == 4 ? 2 : 3); ++i) {
-      const R t2 = t * t, t3 = t2 * t;
-      const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha +
-                  (R(3) * t2 - R(2) * t3) * xb + (t3 - t2) * hb;
+    R phie, we;  // angle from the camera and w = du/dphi at the escape radius
+    if (!escape_by_integral(st, c, &phie, &we)) {
+      // Cubic Hermite through (xa, wa) and (x, w) over the last step; Newton
+      // for the parameter t where x(t) = x_esc.
+      const R xa = st.xa, xb = st.x, ha = c.h * st.wa, hb = c.h * st.w, xe = c.x_esc;
+      R t = shade_div(xa - xe, xa - xb);
+      t = fmin(fmax(t, R(0)), R(1));
+      for (int i = 0; i < (sizeof(R) == 4 ? 2 : 3); ++i) {
+        const R t2 = t * t, t3 = t2 * t;
+        const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha +
+                    (R(3) * t2 - R(2) * t3) * xb + (t3 - t2) * hb;
+        const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
+                     (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
+        t = fmin(fmax(t - shade_div(p - xe, dp), R(0)), R(1));
+      }
+      const R t2 = t * t;
       const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
                    (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
-      t = fmin(fmax(t - shade_div(p - xe, dp), R(0)), R(1));
+      we = shade_div(dp, c.h);
+      phie = (R(st.k - 1) + t) * c.h;
     }
-    const R t2 = t * t;
-    const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
-                 (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
-    const R we = shade_div(dp, c.h);
-    const R phie = (R(st.k - 1) + t) * c.h;  // from the camera
     // direction angle psi = phie + atan2(u, -w) (from the radial direction,
     // measured from yv toward xv); its cosine and sine without atan2
     hit.cls = BH_CLASS_MISS;
@@ -893,6 +964,10 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
 // ---------------------------------------------------------------------------
 // per-ray drivers
 constexpr double kBC = 5.196152422706632;  // 3 sqrt(3)
+// The mixed FP32 pass keeps (x, w) on the first integral near the photon
+// sphere only for rays with |b - b_c| < kProjectBand M: elsewhere the FP32
+// drift of eps moves the deflection by < 3e-6 M / |b - b_c| < 1e-5 rad.
+constexpr float kProjectBand = 0.3f;
 
 // Full trace in one precision R.
 template <typename R, bool kMixed>
@@ -1183,32 +1258,117 @@ __device__ Hit trace_multi(const DevScene& s, int px, int py, const Rk4Consts<R>
   return trace_multi_n<R, 0>(s, px, py, c, steps);
 }
 
-// FP64 trace of a band ray (out of line: keeps FP64 register pressure away
-// from the FP32 callers).
-__device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
-  return trace_rk4<double, false>(s, x, y, p.cband, steps);
+// The FP64 band pass's integration, in double-float on the FP32 pipe: the
+// loop of advance_rk4 (blocks of 4 steps with one event test, then single
+// steps to the event or the next crossing's step) over a state of two floats
+// each, with the band step's constants split on the host. Setup, crossings
+// and the escape stay in FP64 (once per ray or event), on the state converted
+// exactly to double. Double-float rounding (~2^-48) is amplified like FP64's
+// (2^-53) near the photon orbit: against the FP64 integration of the same
+// step it errs ~1e-7 rad at |b - b_c| = 1e-6 M and ~1e-6 rad at 1e-8 M, so
+// rays with |b - b_c| below ~1e-7 M stay in FP64 (band_needs_fp64). The state
+// is not projected onto the first integral: RK4's own truncation moves that
+// integral, and a projected trajectory leaves the FP64 one by ~2e-11 / |b - b_c|
+// rad at the band step 0.01.
+__device__ __forceinline__ int advance_band_df(const DevScene& s, RayState<double>& st, const Rk4Consts<double>& c,
+                                               const LaunchParams& p, int budget) {
+  DF k[6];
+  for (int i = 0; i < 6; ++i) k[i] = DF{p.band_df[i][0], p.band_df[i][1]};
+  const DF x_esc{p.band_df[6][0], p.band_df[6][1]}, x_hor{p.band_df[7][0], p.band_df[7][1]};
+  int taken = 0;
+  while (st.status == kRunning) {
+    if (st.k >= c.kmax) {
+      st.status = kMaxSteps;
+      break;
+    }
+    if (st.k == st.kc) {
+      if (cross_disc<double, false>(s, st, c.h)) {
+        st.status = kDisc;
+        break;
+      }
+    }
+    if (taken >= budget) break;
+    const int kstop = min(min(st.kc, c.kmax), st.k + (budget - taken));
+    DF x = df_from(st.x), w = df_from(st.w);
+    int kk = st.k;
+    while (kk + 4 <= kstop) {
+      const DF x0 = x, w0 = w;
+      df_rk4_step(x, w, k);
+      df_rk4_step(x, w, k);
+      df_rk4_step(x, w, k);
+      df_rk4_step(x, w, k);
+      if (!(df_lt(x_esc, x) && df_lt(x, x_hor))) {
+        x = x0;
+        w = w0;
+        break;
+      }
+      kk += 4;
+    }
+    DF xa = x, wa = w;
+    int ev = kRunning;
+    while (kk < kstop) {
+      xa = x;
+      wa = w;
+      df_rk4_step(x, w, k);
+      ++kk;
+      if (!(df_lt(x_esc, x) && df_lt(x, x_hor))) {  // also NaN
+        ev = df_le(x, x_esc) ? kEscape : kHorizon;
+        break;
+      }
+    }
+    taken += kk - st.k;
+    st.k = kk;
+    st.x = df_to(x);
+    st.w = df_to(w);
+    st.xa = df_to(xa);
+    st.wa = df_to(wa);
+    st.status = ev;
+  }
+  return taken;
 }
 
-// First integral eps = 1/(b/M)^2 - 1/27 of pixel (x, y) in FP64:
-// b = |F x e| / |e| with e = F - pv, so (b/M)^-2 = |e|^2 M^2 / |F x e|^2
-// (about 25 FP64 operations, no square root).
-__device__ __noinline__ double eps_fp64(const DevScene& s, int x, int y) {
-  const V3<double> F = {s.F[0], s.F[1], s.F[2]};
-  const double a = s.half_w - double(x), c = s.half_h - double(y);
-  const V3<double> e = V3<double>{s.E0[0], s.E0[1], s.E0[2]} + V3<double>{s.vy[0], s.vy[1], s.vy[2]} * a +
-                       V3<double>{s.vz[0], s.vz[1], s.vz[2]} * c;
-  const V3<double> fe = cross(F, e);
-  return dot(e, e) * (s.mass * s.mass) / dot(fe, fe) - 1.0 / 27.0;
+// Band rays whose first integral lies within ~1.5e-9 of the photon orbit's
+// (|b - b_c| < ~1e-7 M) integrate in FP64, the rest in double-float.
+__device__ __forceinline__ bool band_needs_fp64(const RayState<double>& st) { return fabs(st.eps) < 1.5e-9; }
+
+// One band slice: up to `budget` steps in the precision the ray needs.
+__device__ __forceinline__ int advance_band(const DevScene& s, RayState<double>& st, const Rk4Consts<double>& c,
+                                            const LaunchParams& p, int budget) {
+  if (band_needs_fp64(st)) return advance_rk4<double, false>(s, st, c, budget);
+  return advance_band_df(s, st, c, p, budget);
+}
+
+// Trace of a band ray: FP64 setup and events, the integration of
+// advance_band (out of line: keeps its register pressure away from the FP32
+// callers).
+__device__ __noinline__ Hit trace_band(const DevScene& s, int x, int y, const LaunchParams& p, int* steps) {
+  RayState<double> st;
+  init_rk4<double>(s, make_ray_rk4<double>(s, x, y), p.cband.h, st);
+  *steps = advance_band(s, st, p.cband, p, 0x7fffffff);
+  return finish_rk4<double>(s, st, p.cband);
+}
+
+// First integral eps = 1/(b/M)^2 - 1/27 of pixel (x, y), exact to double-float
+// (~1e-13 relative): b = |F x e| / |e|, so (b/M)^-2 = M^2 |e|^2 / |F x e|^2,
+// both squares evaluated from their per-scene quadratic forms in the pixel
+// offsets (resolve_derived). About 200 FP32 instructions, where the same in
+// FP64 took ~25 FP64 instructions of ~64 issue cycles each. Every operation is
+// an explicitly rounded double-float step (no contraction the compiler could
+// choose differently), so each kernel that inlines this and decides the FP64
+// band with it takes the same decision for every ray.
+__device__ __forceinline__ DF eps_df(const DevScene& s, int x, int y) {
+  const float a = s.half_w_f - float(x), c = s.half_h_f - float(y);  // exact: half sizes are k / 2
+  return df_first_integral(df_quad_form(s.eq_e, a, c), df_quad_form(s.eq_g, a, c), DF{s.m2_df[0], s.m2_df[1]});
 }
 
 // The FP64 band test of the mixed tracer: an FP32 prefilter on b, then the
-// FP64 first integral of the candidates. setup_mixed and the classification
+// exact first integral of the candidates. setup_mixed and the classification
 // pass make the same decision (same code, same ray).
 __device__ __forceinline__ bool band_candidate(const DevScene& s, const RkRay<float>& r, const LaunchParams& p) {
   return fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band;
 }
-__device__ __forceinline__ bool in_band_eps(double eps, const LaunchParams& p) {
-  return eps > p.eps_band_lo && eps < p.eps_band_hi;
+__device__ __forceinline__ bool in_band_eps(DF eps, const LaunchParams& p) {
+  return df_lt(DF{p.eps_band_df[0], p.eps_band_df[1]}, eps) && df_lt(eps, DF{p.eps_band_df[2], p.eps_band_df[3]});
 }
 
 // Sets up one ray of the mixed tracer. Returns false when the ray belongs to
@@ -1219,14 +1379,15 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
                                             RayState<float>& st) {
   const RkRay<float> r = make_ray_rk4<float>(s, x, y);
   init_rk4<float>(s, r, p.c32.h, st);
+  st.near = fabsf(r.b * s.inv_mass_f - float(kBC)) < kProjectBand;
   if (band_candidate(s, r, p)) {
-    const double eps = eps_fp64(s, x, y);
+    const DF eps = eps_df(s, x, y);
     if (in_band_eps(eps, p)) {
       st.status = kDone;
       return false;
     }
     if (st.status == kRunning) {
-      st.eps = float(eps);
+      st.eps = eps.hi;
       st.w = copysignf(sqrtf(fmaxf(st.eps + st.x * st.x * fmaf(2.f, st.x, 1.f), 0.f)), st.w);
     }
   }
@@ -1503,8 +1664,8 @@ __device__ __forceinline__ long long pixel_ray(const DevScene& s, int x, int y) 
 // Sort key of a band ray: a near-critical ray winds about -ln|eps| / (2 pi)
 // times before it leaves, so its length grows with -log2 |eps|. Four keys per
 // octave of |eps| below the band's edge; the last key takes the rest.
-__device__ __forceinline__ int band_key(double eps, const LaunchParams& p) {
-  const float ae = fmaxf(fabsf(float(eps)) * p.band_key_scale, 1e-30f);
+__device__ __forceinline__ int band_key(float eps, const LaunchParams& p) {
+  const float ae = fmaxf(fabsf(eps) * p.band_key_scale, 1e-30f);
   return (int)fminf(float(kBandKeys - 1), fmaxf(0.f, -__log2f(ae) * 4.f));
 }
 
@@ -1546,11 +1707,11 @@ __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
         if (x >= s.width) continue;
         const RkRay<float> r = make_ray_rk4<float>(s, x, y);
         if (!(fabsf(r.b * s.inv_mass_f - float(kBC)) < p.class_band)) continue;
-        const double eps = eps_fp64(s, x, y);
+        const DF eps = eps_df(s, x, y);
         if (!in_band_eps(eps, p)) continue;
         const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
         if (slot < p.band_capacity) {
-          const int key = band_key(eps, p);
+          const int key = band_key(eps.hi, p);
           p.band_tmp[slot] = (uint32_t)pixel_ray(s, x, y);
           p.band_key[slot] = (uint8_t)key;
           atomicAdd(&p.counters->band_hist[key], 1u);
@@ -1687,7 +1848,8 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
     // GRID schedule does) measured 3.5 % slower on the 120-frame fly-through
     if (st.status != kDone) {
       const DevScene& s = p.scenes[scene];
-      steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
+      if constexpr (kPass == 2) steps += advance_band(s, st, c, p, p.slice_steps);
+      else steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
       if (st.status != kRunning) {
         store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c));
         st.status = kDone;
@@ -1736,6 +1898,17 @@ __global__ void __launch_bounds__(256) persistent_band_kernel(LaunchParams p) {
     if (cudaGetLastError() != cudaSuccess) atomicOr(&p.counters->flags, kFlagBandLaunchFailed);
   }
   persistent_body<2>(p);
+}
+
+// Grid of the band classification: scenes along y; along x, blocks of 256
+// threads for about 8 of an average scene's 32-pixel row segments per thread
+// (a grid-stride loop covers larger scenes). One thread per segment took ~30
+// waves of short blocks on the 120-frame 1080p fly-through, ~0.1 ms of block
+// scheduling before the FP32 pass could start.
+dim3 classify_grid(const LaunchParams& q, int sms) {
+  const long long per_scene = q.total_rays / 32 / std::max(1, q.n_scenes);
+  const long long gx = (per_scene + 256 * 8 - 1) / (256 * 8);
+  return dim3(unsigned(std::max(1ll, std::min<long long>(gx, 2ll * sms))), unsigned(std::min(q.n_scenes, 65535)));
 }
 
 // ---------------------------------------------------------------------------
@@ -1843,9 +2016,7 @@ cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cu
     LaunchParams q = p;
     q.mixed_blocks = p.band_serial ? 0 : blocks;
     const int band_blocks = std::max(1, std::min(blocks, sms));
-    // classification: scenes along y, 32-pixel row segments along x
-    const dim3 cg(std::max(1, std::min(sms * 2, 1024)), std::min(q.n_scenes, 65535));
-    classify_band_kernel<<<cg, 256, 0, stream>>>(q);
+    classify_band_kernel<<<classify_grid(q, sms), 256, 0, stream>>>(q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sort_band_kernel<<<sms, 256, 0, stream>>>(q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1883,8 +2054,7 @@ cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const i
   q.mixed_blocks = p.band_serial ? 0 : 1;  // nonzero: the FP64 pass launches the FP32 pass
   q.drain_only = 0;
   const dim3 grid(q.grid_dim[0], q.grid_dim[1], q.grid_dim[2]), block(block_x, block_y, 1);
-  const dim3 cg(std::max(1, std::min(sms * 2, 1024)), std::min(q.n_scenes, 65535));
-  classify_band_kernel<<<cg, 256, 0, stream>>>(q);
+  classify_band_kernel<<<classify_grid(q, sms), 256, 0, stream>>>(q);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   sort_band_kernel<<<sms, 256, 0, stream>>>(q);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

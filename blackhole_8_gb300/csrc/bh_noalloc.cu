@@ -155,6 +155,7 @@ void resolve(const bh_scene& s, const bh_frame& f, const bh_render_options& o, c
   d->inv_mass_f = float(1.0 / d->mass);
   d->b_lip = bhgb::row_b_lipschitz(d->F, d->E0, d->vy, d->vz, d->mass);
   bhgb::resolve_rk4_constants(d->Fhat, d->Fhat_f, &d->Flen, &d->Flen_f, &d->x0, &d->x0_f, d->F, d->mass);
+  bhgb::resolve_derived(d);
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
@@ -282,14 +283,10 @@ extern "C" int bh_render_noalloc(int device, const bh_scene* scenes, int32_t n, 
   p.c32 = bhgb::make_rk4_consts<float>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.c64 = bhgb::make_rk4_consts<double>(o.step, 1.0 / o.r_escape, o.max_steps);
   p.cband = bhgb::make_rk4_consts<double>(o.band_step, 1.0 / o.r_escape, o.max_steps);
+  bhgb::split_band_consts(p.cband, p.band_df);
   p.setup_band = bhgb::setup_band_for(o.band, o.setup_band);
   p.class_band = bhgb::class_band_for(o.band);
-  {
-    const double bc = 3.0 * std::sqrt(3.0), lo = bc + o.band, hi = bc - o.band;
-    p.eps_band_lo = o.band == 0 ? 0.0 : 1.0 / (lo * lo) - 1.0 / 27.0;
-    p.eps_band_hi = o.band == 0 ? 0.0 : (hi > 0 ? 1.0 / (hi * hi) - 1.0 / 27.0 : 1e300);
-    p.band_key_scale = bhgb::band_key_scale_for(p.eps_band_lo, p.eps_band_hi);
-  }
+  bhgb::set_band_eps(o.band, &p.eps_band_lo, &p.eps_band_hi, &p.band_key_scale, p.eps_band_df);
   p.total_rays = total;
   p.counters = reinterpret_cast<DevCounters*>(base + kCountersOffset);
   bhgb::carve_band(reinterpret_cast<uint32_t*>(base + kBandOffset), uint32_t(BH_NOALLOC_MAX_RAYS), &p.band_list,
