@@ -74,12 +74,14 @@ struct DevScene {
   double s1_len, s2_len;
   double half_w, half_h;      // W / 2.0, H / 2.0
   double Fhat[3], Flen, x0;   // RK4: F / |F|, |F|, M / |F| - 1/3 (the same for every ray)
+  double g0, dnF;             //   x0^2 (1 + 2 x0) (w0^2 = eps + g0), disc normal . F / |F|
 
   float F_f[3], E0_f[3], vy_f[3], vz_f[3];
   float dc_f[3], dn_f[3], dv1_f[3], ds1_f[3], ds2_f[3], de1_f[3], de2_f[3];
   float mass_f, b_c_f, r_h_f, r_in_f, r_out_f, s1_len_f, s2_len_f, half_w_f, half_h_f;
   float inv_mass_f;
   float Fhat_f[3], Flen_f, x0_f;
+  float g0_f, dnF_f;
   float b_lip;                // bound on |b(x+1) - b(x)| / M along an image row (row_b_lipschitz)
   // MIXED, double-float (hi, lo) copies for the FP32 passes' rare exact paths:
   // |e|^2 and |F x e|^2 as quadratic forms in the pixel offsets (a, c), six
@@ -87,6 +89,9 @@ struct DevScene {
   // crossing refinement
   float eq_e[6][2], eq_g[6][2], m2_df[2];
   float mass_df[2], r_in_df[2], r_out_df[2];
+  // FP32 terms every RK4 ray reads, grouped in 16-byte vectors so that a
+  // group is one load (resolve_derived; kHot* indices)
+  float4 hot[10];
   // FP32 polar disc lookup of a disc centred on the hole (resolve_derived)
   int32_t disc_centred;       // 1 when the disc centre is the hole's position
   float disc_tx_scale_f;      // disc texture width / (r_out - r_in)
@@ -113,6 +118,20 @@ struct DevScene {
   uint8_t* pixels;
   uint8_t* cls;
   float* aux;
+};
+
+// The groups of DevScene::hot: (x, y, z, w) of each.
+enum : int {
+  kHotE0 = 0,    // E0, half_w
+  kHotVy = 1,    // vy, half_h
+  kHotVz = 2,    // vz, Flen
+  kHotF = 3,     // F, 1 / M
+  kHotDn = 4,    // disc normal, normal . F^
+  kHotFhat = 5,  // F^, x0
+  kHotMass = 6,  // M, g0, r_in, r_out
+  kHotDe1 = 7,   // polar disc e1, e1 . F^
+  kHotDe2 = 8,   // polar disc e2, e2 . F^
+  kHotDisc = 9,  // disc texture width / (r_out - r_in), -, -, -
 };
 
 // Device-side counters of one render (reset before every render).
@@ -192,7 +211,7 @@ struct LaunchParams {
   int32_t refill_threshold;
   int32_t slice_steps;
   int32_t band_lanes;
-  int32_t band_serial;        // persistent MIXED: 1 = FP32 pass, then FP64 pass, from the host
+  int32_t band_serial;        // MIXED: 1 = FP32 pass, then FP64 pass; 2 = FP64 pass, then FP32 pass (from the host)
   int32_t mixed_blocks;       // persistent MIXED: grid of the FP32 pass the FP64 pass launches (0: none)
   int32_t rays_per_thread;    // GRID: consecutive block tiles down the image per block (>= 1)
   int32_t hybrid;             // HYBRID MIXED: the FP32 pass is grid_kernel with band rays deferred
@@ -219,15 +238,17 @@ inline float row_b_lipschitz(const double F[3], const double E0[3], const double
 }
 
 // The FP32 prefilters on b of the mixed tracer. A band ray has
-// |b - b_c| < band in FP64, and b in FP32 (make_ray) differs from it by
-// ~1e-5 M at most. The classification tests the rays within band + 1e-3 M,
-// the FP32 pass's setup the rays within setup_band, raised to band + 2e-3 M
-// when smaller. Both edges then lie at least 1e-3 M outside the FP64 band, so
-// the two kernels (each with its own compiled make_ray) take the same
-// decision for every ray: only the FP64 band test, the same code in both,
-// decides. The classification then skips the FP64 test for most rays near
-// b_c.
-inline float class_band_for(double band) { return band > 0 ? float(band + 1e-3) : 0.f; }
+// |b - b_c| < band exactly, and b in FP32 differs from it by at most
+// ~1.2e-7 |F| (the rounding of the ray direction e = E0 + a vy + c vz) plus
+// ~2e-7 b (the cross product and the norms): ~5e-6 M with the camera at 30 M.
+// The classification tests the rays within band + 1e-4 M + 1e-6 |F| (its
+// per-scene term added in the kernel), the FP32 pass's setup the rays within
+// setup_band, raised to band + 2e-3 M when smaller. Both edges lie far
+// outside the FP64 band by more than that rounding, so the two kernels (each
+// with its own FP32 b) take the same decision for every ray: only the exact
+// band test, the same code in both, decides. The classification then skips
+// the exact test for all but a ring about two pixels wide around b_c.
+inline float class_band_for(double band) { return band > 0 ? float(band + 1e-4) : 0.f; }
 inline float setup_band_for(double band, double setup_band) {
   return float(band > 0 && band + 2e-3 > setup_band ? band + 2e-3 : setup_band);
 }
@@ -260,8 +281,8 @@ inline void split_df(double v, float* out) {
 }
 
 // Per-scene values derived from a resolved scene (mass, radii, disc basis,
-// textures, camera vectors and RK4 constants set): the double-float copies
-// and the FP32 polar disc lookup's constants. With the pixel offsets a = W/2 - x, c = H/2 - y, the ray direction is
+// textures, camera vectors and RK4 constants set): the double-float copies,
+// the RK4 setup's per-scene terms and the FP32 polar disc lookup's constants. With the pixel offsets a = W/2 - x, c = H/2 - y, the ray direction is
 // e = E0 + a vy + c vz, so |e|^2 and |F x e|^2 = |G0 + a G1 + c G2|^2 (Gi = F x
 // E0, F x vy, F x vz) are quadratic forms in (a, c); their coefficients, in
 // the order of Q = k0 + a (k1 + a k3) + c (k2 + a k4 + c k5), are formed here
@@ -288,10 +309,25 @@ inline void resolve_derived(DevScene* d) {
   split_df(d->mass, d->mass_df);
   split_df(d->r_in, d->r_in_df);
   split_df(d->r_out, d->r_out_df);
+  d->g0 = d->x0 * d->x0 * (1.0 + 2.0 * d->x0);
+  d->g0_f = float(d->g0);
+  d->dnF = dot(d->dn, d->Fhat);
+  d->dnF_f = float(d->dnF);
   d->disc_centred = d->dc[0] == 0 && d->dc[1] == 0 && d->dc[2] == 0 ? 1 : 0;
   d->disc_tx_scale_f = d->r_out > d->r_in ? float(d->disc_tex.width / (d->r_out - d->r_in)) : 0.f;
   d->de1F_f = float(dot(d->de1, d->Fhat));
   d->de2F_f = float(dot(d->de2, d->Fhat));
+  auto f4 = [](const float* v, float w) { return float4{v[0], v[1], v[2], w}; };
+  d->hot[kHotE0] = f4(d->E0_f, d->half_w_f);
+  d->hot[kHotVy] = f4(d->vy_f, d->half_h_f);
+  d->hot[kHotVz] = f4(d->vz_f, d->Flen_f);
+  d->hot[kHotF] = f4(d->F_f, d->inv_mass_f);
+  d->hot[kHotDn] = f4(d->dn_f, d->dnF_f);
+  d->hot[kHotFhat] = f4(d->Fhat_f, d->x0_f);
+  d->hot[kHotMass] = float4{d->mass_f, d->g0_f, d->r_in_f, d->r_out_f};
+  d->hot[kHotDe1] = f4(d->de1_f, d->de1F_f);
+  d->hot[kHotDe2] = f4(d->de2_f, d->de2F_f);
+  d->hot[kHotDisc] = float4{d->disc_tx_scale_f, 0.f, 0.f, 0.f};
 }
 
 // The band step's constants in double-float (the band pass integrates in
@@ -441,7 +477,7 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
   if (o.slice_steps < 4 || o.slice_steps > 4096)
     return bad(BH_ERR_INVALID_ARGUMENT, "slice_steps must be in [4, 4096]");
   if (o.band_lanes < 1 || o.band_lanes > 32) return bad(BH_ERR_INVALID_ARGUMENT, "band_lanes must be in [1, 32]");
-  if (o.band_serial != 0 && o.band_serial != 1) return bad(BH_ERR_INVALID_ARGUMENT, "band_serial must be 0 or 1");
+  if (o.band_serial < 0 || o.band_serial > 2) return bad(BH_ERR_INVALID_ARGUMENT, "band_serial must be 0, 1 or 2");
   if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
     return bad(BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
   if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
@@ -484,11 +520,13 @@ cudaError_t launch_grid(const LaunchParams& p, const int32_t* scene_w, const int
 // MIXED: classifies the FP64-band rays, runs the FP64 pass, which launches
 // the FP32 pass from the device once all its blocks are resident, then a
 // host-launched FP32 pass that drains what is left of the ray queue
-// (band_serial: the FP32 pass, then the FP64 pass, both from the host).
+// (band_serial 1: the FP32 pass, then the FP64 pass, both from the host;
+// 2: the FP64 pass without its device-side launch, then the FP32 pass).
 cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cudaStream_t stream);
 // HYBRID: as launch_persistent, with the FP32 pass on the GRID schedule
 // (rays_per_thread block tiles per block, band rays deferred); the host's
-// launch after the FP64 pass traces only if the device-side launch failed.
+// launch after the FP64 pass, one wave of blocks looping over the frame
+// blocks, traces only if the FP64 pass did not launch the FP32 pass.
 // FP32 precision: launch_grid.
 cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const int32_t* scene_h, int block_x,
                           int block_y, int band_threads, cudaStream_t stream);

@@ -80,6 +80,7 @@ __device__ __forceinline__ V3<R> normalize(V3<R> a) {
 }
 template <typename R, typename S>
 __device__ __forceinline__ V3<R> cast3(V3<S> a) { return {R(a.x), R(a.y), R(a.z)}; }
+__device__ __forceinline__ V3<float> xyz(float4 v) { return {v.x, v.y, v.z}; }
 
 // Precision-dependent view of a DevScene field.
 template <typename R>
@@ -204,10 +205,11 @@ __device__ uchar4 disc_color_polar(const DevScene& s, V3<R> hit) {
 __device__ __forceinline__ uchar4 disc_color_polar_centred(const DevScene& s, float rw, float cp, float sp,
                                                            V3<float> xv) {
   const int W = s.disc_tex.width, H = s.disc_tex.height;
-  int tx = (int)floorf((rw - s.r_in_f) * s.disc_tx_scale_f);
+  const float4 e1 = s.hot[kHotDe1], e2 = s.hot[kHotDe2];
+  int tx = (int)floorf((rw - s.hot[kHotMass].z) * s.hot[kHotDisc].x);
   tx = min(max(tx, 0), W - 1);
-  const float y = fmaf(cp, s.de2F_f, sp * dot(BH_V(float, s, de2), xv));
-  const float x = fmaf(cp, s.de1F_f, sp * dot(BH_V(float, s, de1), xv));
+  const float y = fmaf(cp, e2.w, sp * dot(xyz(e2), xv));
+  const float x = fmaf(cp, e1.w, sp * dot(xyz(e1), xv));
   float a = atan2_poly(y, x) * 0.159154943f;  // 1 / (2 pi)
   a -= floorf(a);
   int ty = (int)floorf(a * float(H));
@@ -310,13 +312,31 @@ struct RkRay {
   R F1, b;
 };
 
+// The scene terms of the RK4 ray setup: in FP32 four 16-byte loads of the
+// scene's hot groups, in FP64 the exact fields.
+template <typename R>
+struct RaySetupScene {
+  V3<R> E0, vy, vz, F;
+  R half_w, half_h, Flen, inv_mass;
+};
+template <typename R>
+__device__ __forceinline__ RaySetupScene<R> ray_setup_scene(const DevScene& s) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 e0 = s.hot[kHotE0], vy = s.hot[kHotVy], vz = s.hot[kHotVz], f = s.hot[kHotF];
+    return {xyz(e0), xyz(vy), xyz(vz), xyz(f), e0.w, vy.w, vz.w, f.w};
+  } else {
+    return {BH_V(R, s, E0), BH_V(R, s, vy), BH_V(R, s, vz), BH_V(R, s, F), s.half_w, s.half_h, s.Flen, 1.0 / s.mass};
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ RkRay<R> make_ray_rk4(const DevScene& s, int x, int y) {
-  const R a = BH_S(R, s, half_w) - R(x);
-  const R c = BH_S(R, s, half_h) - R(y);
-  const V3<R> yv = normalize(BH_V(R, s, E0) + BH_V(R, s, vy) * a + BH_V(R, s, vz) * c);
-  const R L = BH_S(R, s, Flen);
-  const V3<R> F = BH_V(R, s, F);
+  const RaySetupScene<R> q = ray_setup_scene<R>(s);
+  const R a = q.half_w - R(x);
+  const R c = q.half_h - R(y);
+  const V3<R> yv = normalize(q.E0 + q.vy * a + q.vz * c);
+  const R L = q.Flen;
+  const V3<R> F = q.F;
   const V3<R> fx = cross(F, yv);
   RkRay<R> r;
   r.F1 = dot(yv, F);
@@ -691,28 +711,31 @@ struct RayState {
                 // camera: position = r (cos(phi - phi0) F^ + sin(phi - phi0) xv)
 };
 
-// Sets up the RK4 state from a plane ray computed in precision RS.
-template <typename R>
-__device__ __forceinline__ R inv_mass(const DevScene& s);
-template <>
-__device__ __forceinline__ float inv_mass<float>(const DevScene& s) { return s.inv_mass_f; }
-template <>
-__device__ __forceinline__ double inv_mass<double>(const DevScene& s) { return 1.0 / s.mass; }
-
 // Sets up the RK4 state of a ray; everything in precision R. The camera sits
 // at angle phi0 = atan2(b, F1) from the ray direction; the basis rotated by
 // phi0 (F^, X0) measures every later angle from the camera, so phi0 itself is
 // only needed for the aux output.
 template <typename R>
 __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray, R h, RayState<R>& st) {
-  const R M = BH_S(R, s, mass);
+  R M, inv_m, x0, g0;
+  if constexpr (sizeof(R) == 4) {
+    const float4 m = s.hot[kHotMass];
+    M = m.x;
+    g0 = m.y;
+    inv_m = s.hot[kHotF].w;
+    x0 = s.hot[kHotFhat].w;
+  } else {
+    M = s.mass;
+    g0 = s.g0;
+    inv_m = 1.0 / s.mass;
+    x0 = s.x0;
+  }
   st.k = 0;
   st.kc = 0x7fffffff;
   st.near = false;
   st.dcr = R(0);
   st.ev = R(0);
-  const R bm = ray.b * inv_mass<R>(s);
-  const R x0 = BH_S(R, s, x0);
+  const R bm = ray.b * inv_m;
   st.xv = ray.X0;
   st.phi0 = s.aux ? atan2(ray.b, ray.F1) : R(0);
   st.x = x0;
@@ -725,11 +748,18 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
   const R mb = shade_div(M, ray.b);
   const R eps = mb * mb - R(1.0 / 27.0);
   st.eps = eps;
-  st.w = copysign(sqrt(fmax(eps + x0 * x0 * fma(R(2), x0, R(1)), R(0))), ray.F1);
+  st.w = copysign(sqrt(fmax(eps + g0, R(0))), ray.F1);  // g0 = x0^2 (1 + 2 x0)
   st.status = kRunning;
   if (s.disc_on) {
-    const V3<R> n = BH_V(R, s, dn);
-    const R A = dot(n, BH_V(R, s, Fhat)), B = dot(n, st.xv);
+    R A, B;
+    if constexpr (sizeof(R) == 4) {
+      const float4 n = s.hot[kHotDn];
+      A = n.w;
+      B = dot(xyz(n), st.xv);
+    } else {
+      A = s.dnF;
+      B = dot(BH_V(R, s, dn), st.xv);
+    }
     if (A * A + B * B > R(1e-24)) {
       // the line of nodes: crossings at d + j pi, d in (0, pi]
       R d = shade_atan2(B, A) + kPi<R>() * R(0.5);
@@ -904,8 +934,47 @@ __device__ __forceinline__ bool escape_by_integral(const RayState<R>& st, const 
   }
 }
 
-// Shades a finished RK4 ray.
+// Escape point by interpolation: cubic Hermite through (xa, wa) and (xb, wb)
+// over the last step (step k, length h), Newton for the parameter t where
+// x(t) = x_esc; returns the angle from the camera and w there.
 template <typename R>
+struct EscapePoint {
+  R phie, we;
+};
+template <typename R>
+__device__ __forceinline__ EscapePoint<R> escape_hermite(R xa, R wa, R xb, R wb, int k, R h, R xe) {
+  const R ha = h * wa, hb = h * wb;
+  R t = shade_div(xa - xe, xa - xb);
+  t = fmin(fmax(t, R(0)), R(1));
+  for (int i = 0; i < (sizeof(R) == 4 ? 2 : 3); ++i) {
+    const R t2 = t * t, t3 = t2 * t;
+    const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha + (R(3) * t2 - R(2) * t3) * xb +
+                (t3 - t2) * hb;
+    const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha + (R(6) * t - R(6) * t2) * xb +
+                 (R(3) * t2 - R(2) * t) * hb;
+    t = fmin(fmax(t - shade_div(p - xe, dp), R(0)), R(1));
+  }
+  const R t2 = t * t;
+  const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha + (R(6) * t - R(6) * t2) * xb +
+               (R(3) * t2 - R(2) * t) * hb;
+  return EscapePoint<R>{(R(k - 1) + t) * h, shade_div(dp, h)};
+}
+// The same and the general disc colour as calls: finish_rk4's rare paths out
+// of line (the plain tracers measured faster so: the FP32 grid kernel at
+// step 0.01 29.0 ms against 32.4 ms with them inline on the 120-frame
+// fly-through, where the mixed tracer's FP32 pass measured 0.06 ms slower).
+template <typename R>
+__device__ __noinline__ EscapePoint<R> escape_hermite_outlined(R xa, R wa, R xb, R wb, int k, R h, R xe) {
+  return escape_hermite<R>(xa, wa, xb, wb, k, h, xe);
+}
+template <typename R>
+__device__ __noinline__ uchar4 disc_color_outlined(const DevScene& s, V3<R> hit) {
+  return disc_color(s, hit);
+}
+
+// Shades a finished RK4 ray. kRareInline: the interpolated escape and the
+// general disc colour inline (the mixed tracer's FP32 pass) or as calls.
+template <typename R, bool kRareInline = false>
 __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Consts<R>& c) {
   Hit hit = {make_uchar4(0, 0, 0, 255), BH_CLASS_HORIZON, 0.f};
   if (st.status == kMaxSteps) {
@@ -921,29 +990,15 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
       hit.bgra = disc_color_polar_centred(s, float(rw), float(cp), float(sp), cast3<float>(st.xv));
     } else {
       const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
-      hit.bgra = disc_color(s, p);
+      hit.bgra = kRareInline ? disc_color(s, p) : disc_color_outlined<R>(s, p);
     }
   } else if (st.status == kEscape) {
     R phie, we;  // angle from the camera and w = du/dphi at the escape radius
     if (!escape_by_integral(st, c, &phie, &we)) {
-      // Cubic Hermite through (xa, wa) and (x, w) over the last step; Newton
-      // for the parameter t where x(t) = x_esc.
-      const R xa = st.xa, xb = st.x, ha = c.h * st.wa, hb = c.h * st.w, xe = c.x_esc;
-      R t = shade_div(xa - xe, xa - xb);
-      t = fmin(fmax(t, R(0)), R(1));
-      for (int i = 0; i < (sizeof(R) == 4 ? 2 : 3); ++i) {
-        const R t2 = t * t, t3 = t2 * t;
-        const R p = (R(2) * t3 - R(3) * t2 + R(1)) * xa + (t3 - R(2) * t2 + t) * ha +
-                    (R(3) * t2 - R(2) * t3) * xb + (t3 - t2) * hb;
-        const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
-                     (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
-        t = fmin(fmax(t - shade_div(p - xe, dp), R(0)), R(1));
-      }
-      const R t2 = t * t;
-      const R dp = (R(6) * t2 - R(6) * t) * xa + (R(3) * t2 - R(4) * t + R(1)) * ha +
-                   (R(6) * t - R(6) * t2) * xb + (R(3) * t2 - R(2) * t) * hb;
-      we = shade_div(dp, c.h);
-      phie = (R(st.k - 1) + t) * c.h;
+      const EscapePoint<R> e = kRareInline ? escape_hermite<R>(st.xa, st.wa, st.x, st.w, st.k, c.h, c.x_esc)
+                                           : escape_hermite_outlined<R>(st.xa, st.wa, st.x, st.w, st.k, c.h, c.x_esc);
+      phie = e.phie;
+      we = e.we;
     }
     // direction angle psi = phie + atan2(u, -w) (from the radial direction,
     // measured from yv toward xv); its cosine and sine without atan2
@@ -1388,7 +1443,7 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
     }
     if (st.status == kRunning) {
       st.eps = eps.hi;
-      st.w = copysignf(sqrtf(fmaxf(st.eps + st.x * st.x * fmaf(2.f, st.x, 1.f), 0.f)), st.w);
+      st.w = copysignf(sqrtf(fmaxf(st.eps + s.g0_f, 0.f)), st.w);
     }
   }
   return true;
@@ -1464,8 +1519,7 @@ __device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, b
 // The frame of this GRID block and the block's column and row of block tiles
 // in it: blocks enumerate the frames' blocks back to back (block_begin), so
 // a binary search over the frames' first blocks finds it (once per block).
-__device__ __forceinline__ int grid_block_frame(const LaunchParams& p, int* bxi, int* byi) {
-  const long long b = blockIdx.x;
+__device__ __forceinline__ int grid_block_frame(const LaunchParams& p, long long b, int* bxi, int* byi) {
   int lo = 0, hi = p.n_scenes - 1;
   if (p.frame_blocks > 0) {
     // frames of one size: a division instead of a chain of dependent loads
@@ -1509,11 +1563,10 @@ __device__ __forceinline__ void grid_store(const DevScene& s, int format, int x,
 // schedule): FP64 band rays are left to the persistent FP64 pass, which
 // traces and writes them; a drain_only launch (the host's, after the FP64
 // pass) traces only when the FP64 pass could not launch this kernel itself.
-template <int kPrecision, int kIntegrator, bool kDefer = false>
-__global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
-  if (kDefer && p.drain_only && !(p.counters->flags & kFlagBandLaunchFailed)) return;
+template <int kPrecision, int kIntegrator, bool kDefer>
+__device__ __forceinline__ void grid_block(const LaunchParams& p, long long vb) {
   int bxi, byi;
-  const DevScene& s = p.scenes[grid_block_frame(p, &bxi, &byi)];
+  const DevScene& s = p.scenes[grid_block_frame(p, vb, &bxi, &byi)];
   const int x = bxi * blockDim.x + threadIdx.x;
   // every lane stays to the end: BGR8 stores are whole-warp operations
   unsigned long long steps_all = 0, rays = 0, band_rays = 0, band_steps = 0;
@@ -1535,7 +1588,7 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
       RayState<float> st;
       if (setup_mixed(s, x, y, p, st)) {
         steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
-        h = finish_rk4<float>(s, st, p.c32);
+        h = finish_rk4<float, true>(s, st, p.c32);
       } else if (kDefer) {
         deferred = true;
       } else {
@@ -1561,6 +1614,21 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
   }
 }
 
+template <int kPrecision, int kIntegrator, bool kDefer = false>
+__global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
+  if (kDefer && p.drain_only) {
+    // the host's launch after the FP64 pass: about one wave of blocks, which
+    // trace every frame block only when the FP64 pass did not launch this
+    // kernel (band_serial 2, or its device-side launch failed); a launch of
+    // the full grid spent ~0.13 ms on the 120-frame fly-through scheduling
+    // blocks that return at once
+    if (p.mixed_blocks && !(p.counters->flags & kFlagBandLaunchFailed)) return;
+    for (long long vb = blockIdx.x; vb < p.grid_dim[0]; vb += gridDim.x) grid_block<kPrecision, kIntegrator, kDefer>(p, vb);
+    return;
+  }
+  grid_block<kPrecision, kIntegrator, kDefer>(p, blockIdx.x);
+}
+
 
 // GRID schedule for the FLAT and MULTI integrators and for scenes with objects: one
 // kernel per precision and integrator, so that the object code does not
@@ -1570,7 +1638,7 @@ __global__ void __launch_bounds__(256) grid_kernel(LaunchParams p) {
 template <typename R, int kIntegrator>
 __global__ void __launch_bounds__(256) grid_objects_kernel(LaunchParams p) {
   int bxi, byi;
-  const DevScene& s = p.scenes[grid_block_frame(p, &bxi, &byi)];
+  const DevScene& s = p.scenes[grid_block_frame(p, blockIdx.x, &bxi, &byi)];
   const int x = bxi * blockDim.x + threadIdx.x;
   // every lane stays to the end: BGR8 stores are whole-warp operations
   unsigned long long steps_all = 0, rays = 0;
@@ -1672,13 +1740,14 @@ __device__ __forceinline__ int band_key(float eps, const LaunchParams& p) {
 // MIXED: lists the FP64-band rays (global ray indices) before the two passes.
 // Each lane tests one 32-pixel row segment: b / M at the segment's centre
 // (between pixels x0 + 15 and x0 + 16) is within 15.5 b_lip of every pixel's,
-// so only segments whose centre lies within class_band + 15.5 b_lip (+ a
-// rounding margin for the two FP32 evaluations) of b_c / M can hold a band
-// ray. The warp then takes the pixels of each such segment together, one per
-// lane, with the FP32 pass's own test (make_ray's b, then the FP64 band test),
-// so the listed rays are exactly the ones the FP32 pass leaves out. The band
-// is a ring a few pixels wide: the rest of the frame costs one b per 32
-// pixels. The list has one slot per ray of the call.
+// so only segments whose centre lies within the pixels' prefilter + 15.5 b_lip
+// (+ a rounding margin for the two FP32 evaluations) of b_c / M can hold a
+// band ray. The warp then takes the pixels of each such segment together, one
+// per lane: an FP32 b within the prefilter (class_band_for), then the exact
+// band test the FP32 pass's setup also takes, so the listed rays are exactly
+// the ones the FP32 pass leaves out. The band is a ring a few pixels wide:
+// the rest of the frame costs one b per 32 pixels. The list has one slot per
+// ray of the call.
 __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1689,24 +1758,32 @@ __global__ void __launch_bounds__(256) classify_band_kernel(LaunchParams p) {
     const long long n_segs = (long long)segs_x * s.height;
     const V3<float> F = BH_V(float, s, F), E0 = BH_V(float, s, E0);
     const V3<float> vy = BH_V(float, s, vy), vz = BH_V(float, s, vz);
-    const float reach = p.class_band + 15.5f * s.b_lip + 1e-5f * length(F) * s.inv_mass_f;
+    // the pixels' prefilter: class_band plus the scene's FP32 rounding term
+    const float cband = p.class_band > 0.f ? p.class_band + 1e-6f * length(F) * s.inv_mass_f : 0.f;
+    const float reach = cband + 15.5f * s.b_lip + 1e-5f * length(F) * s.inv_mass_f;
     for (long long base = warp * 32; base < n_segs; base += warps * 32) {
       const long long seg = base + lane;
       bool hit = false;
       if (seg < n_segs) {
-        const int y = (int)(seg / segs_x);
-        const int x0 = (int)(seg - (long long)y * segs_x) << 5;
+        // 32-bit: a scene has at most 1024 x 32768 segments
+        const unsigned y = unsigned(seg) / unsigned(segs_x);
+        const int x0 = int(unsigned(seg) - y * unsigned(segs_x)) << 5;
         const V3<float> e = E0 + vy * (s.half_w_f - (float(x0) + 15.5f)) + vz * (s.half_h_f - float(y));
-        const float bm = length(cross(F, e)) / length(e) * s.inv_mass_f;
+        const V3<float> fe = cross(F, e);
+        const float bm = sqrtf(__fdividef(dot(fe, fe), dot(e, e))) * s.inv_mass_f;  // within ~3e-7 b
         hit = !(fabsf(bm - float(kBC)) > reach);  // NaN counts as a hit
       }
       for (unsigned hits = __ballot_sync(kFull, hit); hits; hits &= hits - 1u) {
-        const long long hseg = base + (__ffs(hits) - 1);
-        const int y = (int)(hseg / segs_x);
-        const int x = ((int)(hseg - (long long)y * segs_x) << 5) + lane;
+        const unsigned hseg = unsigned(base) + unsigned(__ffs(hits) - 1);
+        const int y = int(hseg / unsigned(segs_x));
+        const int x = (int(hseg - unsigned(y) * unsigned(segs_x)) << 5) + lane;
         if (x >= s.width) continue;
-        const RkRay<float> r = make_ray_rk4<float>(s, x, y);
-        if (!(fabsf(r.b * s.inv_mass_f - float(kBC)) < p.class_band)) continue;
+        // b = |F x e| / |e| in FP32 (within ~1e-5 M of make_ray's, far inside
+        // the 1e-3 M between this prefilter's edge and the FP32 pass's)
+        const V3<float> e = E0 + vy * (s.half_w_f - float(x)) + vz * (s.half_h_f - float(y));
+        const V3<float> fe = cross(F, e);
+        const float bm = sqrtf(__fdividef(dot(fe, fe), dot(e, e))) * s.inv_mass_f;
+        if (!(fabsf(bm - float(kBC)) < cband)) continue;
         const DF eps = eps_df(s, x, y);
         if (!in_band_eps(eps, p)) continue;
         const unsigned long long slot = atomicAdd(&p.counters->band_count, 1ull);
@@ -1851,7 +1928,7 @@ __device__ __forceinline__ void persistent_body(const LaunchParams& p) {
       if constexpr (kPass == 2) steps += advance_band(s, st, c, p, p.slice_steps);
       else steps += advance_rk4<R, kPass == 1>(s, st, c, p.slice_steps);
       if (st.status != kRunning) {
-        store_hit(s, p.format, px, py, finish_rk4<R>(s, st, c));
+        store_hit(s, p.format, px, py, finish_rk4<R, kPass == 1>(s, st, c));
         st.status = kDone;
       }
     }
@@ -2020,7 +2097,7 @@ cudaError_t launch_persistent(const LaunchParams& p, int threads, int blocks, cu
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sort_band_kernel<<<sms, 256, 0, stream>>>(q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (p.band_serial) {
+    if (p.band_serial == 1) {
       persistent_mixed_kernel<<<blocks, threads, 0, stream>>>(q);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
       persistent_band_kernel<<<band_blocks, threads, 0, stream>>>(q);
@@ -2058,7 +2135,7 @@ cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const i
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   sort_band_kernel<<<sms, 256, 0, stream>>>(q);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (p.band_serial) {
+  if (p.band_serial == 1) {
     grid_kernel<BH_PRECISION_MIXED, BH_INTEGRATOR_RK4, true><<<grid, block, 0, stream>>>(q);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     persistent_band_kernel<<<sms, band_threads, 0, stream>>>(q);
@@ -2068,7 +2145,8 @@ cudaError_t launch_hybrid(const LaunchParams& p, const int32_t* scene_w, const i
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   LaunchParams d = q;
   d.drain_only = 1;
-  grid_kernel<BH_PRECISION_MIXED, BH_INTEGRATOR_RK4, true><<<grid, block, 0, stream>>>(d);
+  const dim3 drain(unsigned(std::min<int64_t>(blocks, int64_t(sms) * 8)));
+  grid_kernel<BH_PRECISION_MIXED, BH_INTEGRATOR_RK4, true><<<drain, block, 0, stream>>>(d);
   return cudaGetLastError();
 }
 

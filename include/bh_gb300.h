@@ -243,11 +243,14 @@ typedef struct bh_render_options {
                                 checks (default 256) */
   int32_t band_lanes;        /* MIXED + PERSISTENT: lanes per warp that trace
                                 FP64 band rays (1..32, default 32) */
-  int32_t band_serial;       /* MIXED + PERSISTENT: 0 (default) = the FP64 band
-                                pass runs beside the FP32 pass from its start
-                                and launches it from the device; 1 = the FP32
-                                pass, then the FP64 pass, both launched by the
-                                host (each pass on its own, e.g. to profile) */
+  int32_t band_serial;       /* MIXED + PERSISTENT or HYBRID: 0 (default) = the
+                                FP64 band pass runs beside the FP32 pass from
+                                its start and launches it from the device;
+                                1 = the FP32 pass, then the FP64 pass, both
+                                launched by the host (each pass on its own,
+                                e.g. to profile); 2 = the FP64 pass, then the
+                                FP32 pass, both launched by the host (no
+                                launch from the device) */
   int32_t rays_per_thread;   /* GRID: pixels each thread traces, from that many
                                 consecutive block tiles down the image, one
                                 after the other (1..8; 0 = 1, the default) */

@@ -297,28 +297,33 @@ def test_batched_uneven_scenes(renderer):
 @pytest.mark.parametrize("band", [2e-5, 5e-4, 0.05, 0.2])
 def test_mixed_band_order_is_bit_exact(renderer, band, schedule):
     """The FP64 band pass beside the FP32 pass (it launches the FP32 pass
-    from the device) and the serial order (both passes launched by the host)
-    trace every ray with the same code: frames, classes, deflections and
-    counters equal, and no device-side launch failed. Every pixel is traced
-    exactly once: the classification (32-pixel row segments, skipped by a
-    bound on b along the row) lists exactly the rays the FP32 pass leaves
-    out, also when the band is wider than setup_band (0.1 M)."""
+    from the device) and the serial orders (both passes launched by the host:
+    the FP32 pass first, or the FP64 pass first with the FP32 pass as the
+    host's one-wave launch looping over the frame blocks, the path that runs
+    when a device-side launch fails) trace every ray with the same code:
+    frames, classes, deflections and counters equal, and no device-side
+    launch failed. Every pixel is traced exactly once: the classification
+    (32-pixel row segments, skipped by a bound on b along the row) lists
+    exactly the rays the FP32 pass leaves out, also when the band is wider
+    than setup_band (0.1 M)."""
     scenes = S.flythrough(4, 160, 90) + S.flythrough(120, 320, 180)[60:64]
     pixels = sum(s.camera.width() * s.camera.height() for s in scenes)
     res = []
-    for serial in (0, 1):
+    for serial in (0, 1, 2):
         o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, band=band, band_serial=serial, rays_per_thread=3)
         res.append((renderer.render(scenes, o, hit_class=True, aux=True), renderer.stats()))
-    (a, sa), (b, sb) = res
-    for fa, fb in zip(a, b):
-        assert np.array_equal(fa.pixels, fb.pixels)
-        assert np.array_equal(fa.hit_class, fb.hit_class)
-        assert np.array_equal(fa.aux.view(np.uint32), fb.aux.view(np.uint32))
-    assert (sa.rays, sa.steps, sa.band_rays, sa.band_steps) == (sb.rays, sb.steps, sb.band_rays, sb.band_steps)
+    a, sa = res[0]
+    for b, sb in res[1:]:
+        for fa, fb in zip(a, b):
+            assert np.array_equal(fa.pixels, fb.pixels)
+            assert np.array_equal(fa.hit_class, fb.hit_class)
+            assert np.array_equal(fa.aux.view(np.uint32), fb.aux.view(np.uint32))
+        assert (sa.rays, sa.steps, sa.band_rays, sa.band_steps) == (sb.rays, sb.steps, sb.band_rays, sb.band_steps)
+        assert sb.flags == 0
     assert sa.rays == pixels
     if band >= 0.05:
         assert sa.band_rays > 0
-    assert sa.flags == 0 and sb.flags == 0
+    assert sa.flags == 0
     # the same frames through the grid schedule, which tests the band inline
     g = renderer.render(scenes, opts(precision=capi.PRECISION_MIXED, band=band), hit_class=True)
     for fa, fg in zip(a, g):
