@@ -427,6 +427,7 @@ void resolve_scene(bh_ctx* ctx, const bh_scene& s, const bh_frame& f, const bh_r
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
+  bhgb::resolve_frame_flags(d);
 }
 
 int32_t count_objects(const bh_scene* scenes, int32_t n) {

@@ -92,6 +92,7 @@ struct DevScene {
   // FP32 terms every RK4 ray reads, grouped in 16-byte vectors so that a
   // group is one load (resolve_derived; kHot* indices)
   float4 hot[10];
+  int4 hot_i;                 // kScene* flags, width, height, 0 (resolve_frame_flags)
   // FP32 polar disc lookup of a disc centred on the hole (resolve_derived)
   int32_t disc_centred;       // 1 when the disc centre is the hole's position
   float disc_tx_scale_f;      // disc texture width / (r_out - r_in)
@@ -133,6 +134,23 @@ enum : int {
   kHotDe2 = 8,   // polar disc e2, e2 . F^
   kHotDisc = 9,  // disc texture width / (r_out - r_in), -, -, -
 };
+
+// DevScene::hot_i.x flags.
+enum : int {
+  kSceneDisc = 1,           // disc_on
+  kSceneBg = 2,             // has_bg
+  kSceneDiscPolarCentred = 4,  // POLAR mapping of a disc centred on the hole
+  kSceneAux = 8,            // the frame takes aux output
+  kSceneCls = 16,           // the frame takes hit classes
+};
+
+// The flags group of a resolved scene whose frame pointers are set.
+inline void resolve_frame_flags(DevScene* d) {
+  d->hot_i = int4{(d->disc_on ? kSceneDisc : 0) | (d->has_bg ? kSceneBg : 0) |
+                      (d->disc_map == BH_DISC_MAP_POLAR && d->disc_centred ? kSceneDiscPolarCentred : 0) |
+                      (d->aux ? kSceneAux : 0) | (d->cls ? kSceneCls : 0),
+                  d->width, d->height, 0};
+}
 
 // Device-side counters of one render (reset before every render).
 struct DevCounters {

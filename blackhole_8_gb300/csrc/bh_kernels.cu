@@ -82,6 +82,30 @@ template <typename R, typename S>
 __device__ __forceinline__ V3<R> cast3(V3<S> a) { return {R(a.x), R(a.y), R(a.z)}; }
 __device__ __forceinline__ V3<float> xyz(float4 v) { return {v.x, v.y, v.z}; }
 
+// Per-precision scene terms of the RK4 tracers: FP32 from the scene's 16-byte
+// hot groups (one load each), FP64 from the exact fields.
+template <typename R>
+struct DiscRadii {
+  R M, r_in, r_out;
+};
+template <typename R>
+__device__ __forceinline__ DiscRadii<R> disc_radii(const DevScene& s) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 m = s.hot[kHotMass];
+    return {m.x, m.z, m.w};
+  } else {
+    return {s.mass, s.r_in, s.r_out};
+  }
+}
+template <typename R>
+__device__ __forceinline__ V3<R> fhat_of(const DevScene& s) {
+  if constexpr (sizeof(R) == 4) {
+    return xyz(s.hot[kHotFhat]);
+  } else {
+    return {s.Fhat[0], s.Fhat[1], s.Fhat[2]};
+  }
+}
+
 // Precision-dependent view of a DevScene field.
 template <typename R>
 struct Pick;
@@ -251,13 +275,15 @@ __device__ __forceinline__ Hit miss_hit() { return {make_uchar4(0, 0, 0, 255), B
 
 // Class and aux outputs of pixel (x, y), where the frame asks for them.
 __device__ __forceinline__ void store_extras(const DevScene& s, int x, int y, const Hit& h) {
-  const long long pix = (long long)y * s.width + x;
-  if (s.cls) s.cls[pix] = (uint8_t)h.cls;
-  if (s.aux) s.aux[pix] = h.aux;
+  const int4 fl = s.hot_i;
+  const long long pix = (long long)y * fl.y + x;
+  if (fl.x & kSceneCls) s.cls[pix] = (uint8_t)h.cls;
+  if (fl.x & kSceneAux) s.aux[pix] = h.aux;
 }
 
 __device__ __forceinline__ void store_hit(const DevScene& s, int format, int x, int y, const Hit& h) {
-  const long long pix = (long long)y * s.width + x;
+  const int4 fl = s.hot_i;
+  const long long pix = (long long)y * fl.y + x;
   uchar4 c = h.bgra;
   c.w = 255;
   if (format == BH_FORMAT_BGRA8) {
@@ -270,8 +296,8 @@ __device__ __forceinline__ void store_hit(const DevScene& s, int format, int x, 
     p[1] = c.y;
     p[2] = c.z;
   }
-  if (s.cls) s.cls[pix] = (uint8_t)h.cls;
-  if (s.aux) s.aux[pix] = h.aux;
+  if (fl.x & kSceneCls) s.cls[pix] = (uint8_t)h.cls;
+  if (fl.x & kSceneAux) s.aux[pix] = h.aux;
 }
 
 // ---------------------------------------------------------------------------
@@ -737,7 +763,8 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
   st.ev = R(0);
   const R bm = ray.b * inv_m;
   st.xv = ray.X0;
-  st.phi0 = s.aux ? atan2(ray.b, ray.F1) : R(0);
+  const int flags = s.hot_i.x;
+  st.phi0 = (flags & kSceneAux) ? atan2(ray.b, ray.F1) : R(0);
   st.x = x0;
   if (!(bm > R(1e-6))) {  // heads into the centre
     st.status = kHorizon;
@@ -750,7 +777,7 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
   st.eps = eps;
   st.w = copysign(sqrt(fmax(eps + g0, R(0))), ray.F1);  // g0 = x0^2 (1 + 2 x0)
   st.status = kRunning;
-  if (s.disc_on) {
+  if (flags & kSceneDisc) {
     R A, B;
     if constexpr (sizeof(R) == 4) {
       const float4 n = s.hot[kHotDn];
@@ -818,11 +845,12 @@ template <typename R, bool kRefine64>
 __device__ __forceinline__ bool cross_disc(const DevScene& s, RayState<R>& st, R h) {
   R u = crossing_u<R>(st, h);
   // on_disc, with the crossing radius kept for the refinement test
-  const R rc = shade_div(BH_S(R, s, mass), u);
-  bool hit = u < R(0.5) && rc >= BH_S(R, s, r_in) && rc <= BH_S(R, s, r_out);
+  const DiscRadii<R> d = disc_radii<R>(s);
+  const R rc = shade_div(d.M, u);
+  bool hit = u < R(0.5) && rc >= d.r_in && rc <= d.r_out;
   if (kRefine64) {
-    const R tol = R(2e-3) * BH_S(R, s, mass);
-    if (fabs(rc - BH_S(R, s, r_in)) < tol || fabs(rc - BH_S(R, s, r_out)) < tol) {
+    const R tol = R(2e-3) * d.M;
+    if (fabs(rc - d.r_in) < tol || fabs(rc - d.r_out) < tol) {
       const CrossU r64 = crossing_u_df(float(st.dcr), st.kc, float(st.x), float(st.w), float(h), s);
       u = R(r64.u);
       hit = r64.hit != 0;
@@ -980,16 +1008,17 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
   if (st.status == kMaxSteps) {
     hit.cls = BH_CLASS_MAXSTEPS;
   } else if (st.status == kDisc) {
+    const int flags = s.hot_i.x;
     const R phic = st.dcr;
-    const R rw = shade_div(BH_S(R, s, mass), st.ev);
+    const R rw = shade_div(disc_radii<R>(s).M, st.ev);
     R sp, cp;
     shade_sincos(phic, &sp, &cp);
     hit.cls = BH_CLASS_DISC;
-    if (s.aux) hit.aux = float(R(1) / st.ev);
-    if (sizeof(R) == 4 && s.disc_map == BH_DISC_MAP_POLAR && s.disc_centred) {
+    if (flags & kSceneAux) hit.aux = float(R(1) / st.ev);
+    if (sizeof(R) == 4 && (flags & kSceneDiscPolarCentred)) {
       hit.bgra = disc_color_polar_centred(s, float(rw), float(cp), float(sp), cast3<float>(st.xv));
     } else {
-      const V3<R> p = BH_V(R, s, Fhat) * (rw * cp) + st.xv * (rw * sp);
+      const V3<R> p = fhat_of<R>(s) * (rw * cp) + st.xv * (rw * sp);
       hit.bgra = kRareInline ? disc_color(s, p) : disc_color_outlined<R>(s, p);
     }
   } else if (st.status == kEscape) {
@@ -1003,13 +1032,14 @@ __device__ Hit finish_rk4(const DevScene& s, const RayState<R>& st, const Rk4Con
     // direction angle psi = phie + atan2(u, -w) (from the radial direction,
     // measured from yv toward xv); its cosine and sine without atan2
     hit.cls = BH_CLASS_MISS;
-    if (s.aux) hit.aux = float(st.phi0 + phie + atan2(c.u_esc, -we) - kPi<R>());
-    if (s.has_bg) {
+    const int flags = s.hot_i.x;
+    if (flags & kSceneAux) hit.aux = float(st.phi0 + phie + atan2(c.u_esc, -we) - kPi<R>());
+    if (flags & kSceneBg) {
       R sp, cp;
       shade_sincos(phie, &sp, &cp);
       const R k = rnorm(we * we + c.u_esc * c.u_esc);
       const R cd = -we * k, sd = c.u_esc * k;
-      const V3<R> d = BH_V(R, s, Fhat) * (cp * cd - sp * sd) + st.xv * (sp * cd + cp * sd);
+      const V3<R> d = fhat_of<R>(s) * (cp * cd - sp * sd) + st.xv * (sp * cd + cp * sd);
       hit.bgra = background_color(s, d);
     }
   }
@@ -1420,7 +1450,7 @@ __device__ __forceinline__ DF eps_df(const DevScene& s, int x, int y) {
 // exact first integral of the candidates. setup_mixed and the classification
 // pass make the same decision (same code, same ray).
 __device__ __forceinline__ bool band_candidate(const DevScene& s, const RkRay<float>& r, const LaunchParams& p) {
-  return fabsf(r.b * s.inv_mass_f - float(kBC)) < p.setup_band;
+  return fabsf(r.b * s.hot[kHotF].w - float(kBC)) < p.setup_band;
 }
 __device__ __forceinline__ bool in_band_eps(DF eps, const LaunchParams& p) {
   return df_lt(DF{p.eps_band_df[0], p.eps_band_df[1]}, eps) && df_lt(eps, DF{p.eps_band_df[2], p.eps_band_df[3]});
@@ -1434,7 +1464,7 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
                                             RayState<float>& st) {
   const RkRay<float> r = make_ray_rk4<float>(s, x, y);
   init_rk4<float>(s, r, p.c32.h, st);
-  st.near = fabsf(r.b * s.inv_mass_f - float(kBC)) < kProjectBand;
+  st.near = fabsf(r.b * s.hot[kHotF].w - float(kBC)) < kProjectBand;
   if (band_candidate(s, r, p)) {
     const DF eps = eps_df(s, x, y);
     if (in_band_eps(eps, p)) {
@@ -1443,7 +1473,7 @@ __device__ __forceinline__ bool setup_mixed(const DevScene& s, int x, int y, con
     }
     if (st.status == kRunning) {
       st.eps = eps.hi;
-      st.w = copysignf(sqrtf(fmaxf(st.eps + s.g0_f, 0.f)), st.w);
+      st.w = copysignf(sqrtf(fmaxf(st.eps + s.hot[kHotMass].y, 0.f)), st.w);
     }
   }
   return true;
@@ -1571,10 +1601,11 @@ __device__ __forceinline__ void grid_block(const LaunchParams& p, long long vb) 
   // every lane stays to the end: BGR8 stores are whole-warp operations
   unsigned long long steps_all = 0, rays = 0, band_rays = 0, band_steps = 0;
   for (int k = 0; k < p.rays_per_thread; ++k) {
+    const int4 fl = s.hot_i;  // flags, width, height
     const int row0 = (byi * p.rays_per_thread + k) * blockDim.y;
-    if (row0 >= s.height) break;  // the same for the whole block
+    if (row0 >= fl.z) break;  // the same for the whole block
     const int y = row0 + threadIdx.y;
-    const bool valid = x < s.width && y < s.height;
+    const bool valid = x < fl.y && y < fl.z;
     Hit h = miss_hit();
     int steps = 0;
     int band_ray = 0;

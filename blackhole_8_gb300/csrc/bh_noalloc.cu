@@ -159,6 +159,7 @@ void resolve(const bh_scene& s, const bh_frame& f, const bh_render_options& o, c
   d->pixels = static_cast<uint8_t*>(f.pixels);
   d->cls = f.hit_class;
   d->aux = f.aux;
+  bhgb::resolve_frame_flags(d);
 }
 
 int check(const bh_scene* scenes, int32_t n, const bh_device_texture* tex, int32_t n_tex, const bh_frame* frames,
