@@ -48,13 +48,13 @@ SCHEDULE_NAMES = {0: "grid", 1: "persistent", 2: "hybrid"}
 # DRAM bytes the tuned tracer's FP32 pass (hybrid schedule, step 0.15, band
 # 2e-5, 8x16 blocks, 8 rays per thread) moves per 120-frame fly-through:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size
-# (24.13 MB read, 943.83 MB written: the BGRA8 frames)
-FLYTHROUGH_DRAM_BYTES = 24.13e6 + 943.83e6
+# (23.06 MB read, 940.25 MB written: the BGRA8 frames)
+FLYTHROUGH_DRAM_BYTES = 23.06e6 + 940.25e6
 # the same launch under ncu --set full: FP32 arithmetic instructions (FFMA +
-# FMUL + FADD lanes per cycle) against the chip's FP32 lane-issue peak, and
-# the FMA pipe's busy fraction
-NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.354
-NCU_FMA_PIPE_FRAC = 0.456
+# FMUL + FADD lanes per cycle, 7,500) against the chip's FP32 lane-issue peak
+# (152 SMs x 128), and the FMA pipe's busy fraction
+NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.385
+NCU_FMA_PIPE_FRAC = 0.469
 # algorithmic bytes per ray: the 4-byte frame store and one 4-byte texel read
 ALGO_BYTES_PER_RAY = 8
 

@@ -36,6 +36,8 @@ def build_scenes(args):
         return S.batched_scenes(args.frames)
     if args.workload == "photon-ring":
         return [S.photon_ring_scene(args.width or 4096)]
+    if args.workload == "impact-grid":
+        return [S.impact_grid_scene(args.width or 4096)]
     if args.workload == "objects":
         return [S.objects_scene(args.width or 640, args.height or 360) for _ in range(args.frames)]
     if args.workload == "flat":
@@ -55,8 +57,8 @@ def write_ppm(path: str, bgra) -> None:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--workload", default="flythrough",
-                    choices=["single", "flythrough", "batched", "photon-ring", "adjoint", "objects", "flat",
-                             "binary"])
+                    choices=["single", "flythrough", "batched", "photon-ring", "impact-grid", "adjoint", "objects",
+                             "flat", "binary"])
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
