@@ -1534,16 +1534,13 @@ __device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
   return uint32_t(h.bgra.x) | (uint32_t(h.bgra.y) << 8) | (uint32_t(h.bgra.z) << 16);
 }
 
-// True when the warp's pixels ((x, y) per lane, `valid` where it lies in the
-// frame) form a block of rows of bw pixels (a power of two, 4 to 32) starting
-// at lane 0's pixel that store_bgr8_words can write. Called by all 32 lanes;
-// the result is the same on every lane.
-__device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, int x, int y, bool valid, int bw) {
-  const int lane = int(lane_id());
-  const int x0 = __shfl_sync(kFull, x, 0), y0 = __shfl_sync(kFull, y, 0);
-  const bool mine = valid && x == x0 + (lane & (bw - 1)) && y == y0 + (lane >> (__ffs(bw) - 1));
-  return __all_sync(kFull, mine) && (x0 & 3) == 0 && (s.width & 3) == 0 &&
-         (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
+// True when store_bgr8_words can write the warp's pixels: the GRID kernels'
+// warps cover whole rows of bw pixels (lane l at (x0 + l % bw, y0 + l / bw),
+// x0 a multiple of bw, so of 4), and then it takes every lane's pixel in the
+// frame (`valid`) and frame rows that start on 4-byte boundaries. Called by
+// all 32 lanes; the result is the same on every lane.
+__device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, bool valid) {
+  return __all_sync(kFull, valid) && (s.hot_i.y & 3) == 0 && (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
 }
 
 // The frame of this GRID block and the block's column and row of block tiles
@@ -1577,8 +1574,8 @@ __device__ __forceinline__ void grid_store(const DevScene& s, int format, int x,
     // pixels, or of 4, 8 or 16 (powers of two dividing 32)
     const int bx = int(blockDim.x), bw = bx < 32 ? bx : 32;
     const bool rows = (bx & 31) == 0 || (bx >= 4 && bx < 32 && (bx & (bx - 1)) == 0);
-    if (rows && bgr8_block_ok(s, x, y, valid, bw)) {
-      store_bgr8_words(s.pixels, s.width, __shfl_sync(kFull, x, 0), __shfl_sync(kFull, y, 0), bw, bgr_word(h));
+    if (rows && bgr8_block_ok(s, valid)) {
+      store_bgr8_words(s.pixels, s.hot_i.y, __shfl_sync(kFull, x, 0), __shfl_sync(kFull, y, 0), bw, bgr_word(h));
       store_extras(s, x, y, h);
       return;
     }
