@@ -103,6 +103,33 @@ def _sweep(b, u_a, u_b):
                           limit=200)[0]
 
 
+def _total_deflection(b):
+    """Deflection of a ray from infinity to infinity (M = 1): twice the
+    sweep from u = 0 to the periapsis, minus pi (the exact orbit integral
+    the oracle's RK4 is checked against below)."""
+    return 2.0 * _sweep_to_turning(b, 0.0, _turning_point(b)) - math.pi
+
+
+def test_orbit_integral_weak_field_series():
+    """Published weak-field expansion (M = 1):
+    alpha = 4/b + (15 pi / 4)/b^2 + (128/3)/b^3 + O(1/b^4); the next term is
+    (3465 pi / 64)/b^4 ~ 170/b^4 (measured: 1.1e-7 at b = 200)."""
+    for b in (200.0, 1000.0, 5000.0):
+        series = 4.0 / b + 15.0 * math.pi / 4.0 / b ** 2 + 128.0 / 3.0 / b ** 3
+        assert abs(_total_deflection(b) - series) < max(300.0 / b ** 4, 1e-12), b
+
+
+def test_orbit_integral_strong_field_limit():
+    """Strong-field limit near the photon sphere (Bozza 2002, Schwarzschild):
+    alpha = -ln(b / b_c - 1) + ln(216 (7 - 4 sqrt 3)) - pi + O(b - b_c)
+    (measured remainder ~4-5 (b / b_c - 1))."""
+    bc = 3.0 * math.sqrt(3.0)
+    bbar = math.log(216.0 * (7.0 - 4.0 * math.sqrt(3.0))) - math.pi
+    for eps in (1e-4, 1e-5, 1e-6):
+        b = bc * (1.0 + eps)
+        assert abs(_total_deflection(b) - (-math.log(eps) + bbar)) < 10.0 * eps, eps
+
+
 @pytest.fixture(scope="module")
 def rk4_single():
     sc = S.single_scene(96, 54)
