@@ -503,8 +503,8 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
   if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64) return bad(BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
   if (o.refill_threshold < 1 || o.refill_threshold > 32)
     return bad(BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");
-  if (o.rays_per_thread < 0 || o.rays_per_thread > 8)
-    return bad(BH_ERR_INVALID_ARGUMENT, "rays_per_thread must be in [0, 8]");
+  if (o.rays_per_thread < 0 || o.rays_per_thread > 128)
+    return bad(BH_ERR_INVALID_ARGUMENT, "rays_per_thread must be in [0, 128]");
   return BH_OK;
 }
 

@@ -251,9 +251,10 @@ typedef struct bh_render_options {
                                 e.g. to profile); 2 = the FP64 pass, then the
                                 FP32 pass, both launched by the host (no
                                 launch from the device) */
-  int32_t rays_per_thread;   /* GRID: pixels each thread traces, from that many
-                                consecutive block tiles down the image, one
-                                after the other (1..8; 0 = 1, the default) */
+  int32_t rays_per_thread;   /* GRID / HYBRID: pixels each thread traces, from
+                                that many consecutive block tiles down the
+                                image, one after the other (1..128; 0 = 1, the
+                                default) */
   int32_t reserved[2];
 } bh_render_options;
 

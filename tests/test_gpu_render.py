@@ -160,7 +160,8 @@ def test_grid_shape_and_rays_per_thread_change_nothing(renderer, precision, inte
     frames of different sizes, so that block tiles overhang the images)."""
     scenes = [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1]]
     ref, ref_st = None, None
-    for bx, by, rpt in [(8, 16, 1), (8, 16, 2), (16, 8, 4), (32, 4, 3), (8, 8, 8), (16, 16, 1)]:
+    for bx, by, rpt in [(8, 16, 1), (8, 16, 2), (16, 8, 4), (32, 4, 3), (8, 8, 8), (16, 16, 1), (8, 16, 64),
+                        (32, 4, 128)]:
         o = opts(precision=precision, integrator=integrator, block_x=bx, block_y=by, rays_per_thread=rpt)
         out = renderer.render(scenes, o, hit_class=True)
         st = renderer.stats()
