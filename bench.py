@@ -46,15 +46,15 @@ CPU_SAMPLE_FRAMES = list(range(0, FRAMES, 15))  # 8 frames
 MAX_DEFLECTION_ERROR = 1e-4
 SCHEDULE_NAMES = {0: "grid", 1: "persistent", 2: "hybrid"}
 # DRAM bytes the tuned tracer's FP32 pass (hybrid schedule, step 0.15, band
-# 2e-5, 8x16 blocks, 8 rays per thread) moves per 120-frame fly-through:
+# 2e-5, 8x16 blocks, 32 rays per thread) moves per 120-frame fly-through:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size
-# (23.06 MB read, 940.25 MB written: the BGRA8 frames)
-FLYTHROUGH_DRAM_BYTES = 23.06e6 + 940.25e6
+# (23.18 MB read, 939.96 MB written: the BGRA8 frames)
+FLYTHROUGH_DRAM_BYTES = 23.18e6 + 939.96e6
 # the same launch under ncu --set full: FP32 arithmetic instructions (FFMA +
-# FMUL + FADD lanes per cycle, 7,500) against the chip's FP32 lane-issue peak
+# FMUL + FADD lanes per cycle, 7,693) against the chip's FP32 lane-issue peak
 # (152 SMs x 128), and the FMA pipe's busy fraction
-NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.385
-NCU_FMA_PIPE_FRAC = 0.469
+NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.395
+NCU_FMA_PIPE_FRAC = 0.477
 # algorithmic bytes per ray: the 4-byte frame store and one 4-byte texel read
 ALGO_BYTES_PER_RAY = 8
 
