@@ -76,8 +76,11 @@ enum {
  * (the step's chord) on every step (GRID schedule, FP32 or FP64). */
 enum { BH_INTEGRATOR_REF_TRAPEZOID = 0, BH_INTEGRATOR_RK4 = 1, BH_INTEGRATOR_FLAT = 2, BH_INTEGRATOR_MULTI = 3 };
 
-/* Arithmetic. MIXED (RK4 only): FP32 bulk, FP64 for rays whose impact
- * parameter lies within `band` of 3*sqrt(3)*M, FP64 disc-crossing refinement. */
+/* Arithmetic. MIXED (RK4 only): FP32 bulk; rays whose impact parameter lies
+ * within `band` of 3*sqrt(3)*M integrate with FP64 accuracy (double-float on
+ * the FP32 pipe, FP64 for the few within ~1e-7 M and for their events); the
+ * first integral of rays within `setup_band` and disc-crossing refinement near
+ * the disc edges exact to double-float. */
 enum { BH_PRECISION_FP32 = 0, BH_PRECISION_FP64 = 1, BH_PRECISION_MIXED = 2 };
 
 /* Ray generation. REF reproduces the reference: the ray runs from the focus
@@ -226,7 +229,9 @@ typedef struct bh_render_options {
   double r_escape;           /* RK4 escape radius in units of M (default 100);
                                 MULTI: in units of the holes' total mass */
   double band;               /* MIXED: rays with |b - 3 sqrt(3) M| < band * M are
-                                traced in FP64 with step band_step (default 5e-4) */
+                                traced with FP64 accuracy (double-float, FP64
+                                within ~1e-7 M) with step band_step
+                                (default 5e-4) */
   int32_t block_x;           /* GRID block shape (default 8 x 16: each warp an
                                 8 x 4 pixel tile) */
   int32_t block_y;
@@ -234,9 +239,10 @@ typedef struct bh_render_options {
   int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
   int32_t refill_threshold;  /* PERSISTENT: refill a warp once this many lanes
                                 are idle (default 32) */
-  double band_step;          /* MIXED: RK4 step of the FP64 band (default 0.01) */
+  double band_step;          /* MIXED: RK4 step of the band (default 0.01) */
   double setup_band;         /* MIXED: rays with |b - 3 sqrt(3) M| < setup_band * M
-                                take their first integral 1/b^2 - 1/27 from FP64
+                                take their first integral 1/b^2 - 1/27 exactly
+                                (double-float)
                                 (default 0.1; raised to band + 2e-3 when
                                 smaller) */
   int32_t slice_steps;       /* PERSISTENT: integration steps between refill
