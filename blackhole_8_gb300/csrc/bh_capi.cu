@@ -1379,7 +1379,9 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
       c.block_x = sh[0];
       c.block_y = sh[1];
       c.rays_per_thread = rpt;
-      c.threads_per_block = 128;
+      // the band pass's block: 256 threads took the impact-parameter grid
+      // (20 % band rays) from 57.9 to 43.6 ms against 128, the fly-through alike
+      c.threads_per_block = 256;
       c.format = BH_FORMAT_BGRA8;
       if ((rc = time_candidate(c))) return rc;
     }
