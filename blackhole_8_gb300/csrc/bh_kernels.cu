@@ -891,16 +891,31 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
     const int kstop = min(min(st.kc, c.kmax), st.k + (budget - taken));
     R x = st.x, w = st.w;
     int k = st.k;
-    // blocks of 4 steps, event test once per block
+    R xa = x, wa = w;
+    int ev = kRunning;
+    // blocks of 4 steps, event test once per block; a block that ends outside
+    // takes the event from its kept states: the first step whose end lies
+    // outside, as single steps would find it (same steps, same order)
     while (k + 4 <= kstop) {
       const R x0 = x, w0 = w;
       rk4_step<R>(x, w, c);
+      const R x1 = x, w1 = w;
       rk4_step<R>(x, w, c);
+      const R x2 = x, w2 = w;
       rk4_step<R>(x, w, c);
+      const R x3 = x, w3 = w;
       rk4_step<R>(x, w, c);
       if (!inside(x, c)) {
-        x = x0;
-        w = w0;
+        if (!inside(x1, c)) {
+          xa = x0, wa = w0, x = x1, w = w1, k += 1;
+        } else if (!inside(x2, c)) {
+          xa = x1, wa = w1, x = x2, w = w2, k += 2;
+        } else if (!inside(x3, c)) {
+          xa = x2, wa = w2, x = x3, w = w3, k += 3;
+        } else {
+          xa = x3, wa = w3, k += 4;
+        }
+        ev = x <= c.x_esc ? kEscape : kHorizon;
         break;
       }
       k += 4;
@@ -909,9 +924,7 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
       }
     }
     // single steps up to kstop or the event
-    R xa = x, wa = w;
-    int ev = kRunning;
-    while (k < kstop) {
+    while (ev == kRunning && k < kstop) {
       xa = x;
       wa = w;
       rk4_step<R>(x, w, c);
