@@ -254,7 +254,8 @@ __device__ uchar4 background_color(const DevScene& s, V3<R> d) {
   // angle from the +z pole: pi/2 - asin(z), in FP32 as atan2(|(x, y)|, z)
   R colat;
   if constexpr (sizeof(R) == 4) {
-    colat = atan2_poly(sqrtf(d.x * d.x + d.y * d.y), d.z);
+    const float q2 = d.x * d.x + d.y * d.y;
+    colat = atan2_poly(q2 > 1e-30f ? q2 * rsqrtf(q2) : 0.f, d.z);
   } else {
     colat = kPi<R>() * R(0.5) - asin(fmin(fmax(d.z, R(-1)), R(1)));
   }
@@ -366,8 +367,19 @@ __device__ __forceinline__ RkRay<R> make_ray_rk4(const DevScene& s, int x, int y
   const V3<R> fx = cross(F, yv);
   RkRay<R> r;
   r.F1 = dot(yv, F);
-  r.b = length(fx);
-  const R ilb = r.b > R(0) ? shade_div(R(1), L * r.b) : R(0);
+  R ilb;
+  if constexpr (sizeof(R) == 4) {
+    // b and 1 / (|F| b) from one reciprocal square root (the correctly
+    // rounded square root is a longer dependent sequence on this path;
+    // b errs by ~2 ulp instead of 0.5)
+    const float fx2 = dot(fx, fx);
+    const float rb = fx2 > 1e-30f ? rsqrtf(fx2) : 0.f;
+    r.b = fx2 * rb;
+    ilb = __fdividef(rb, L);
+  } else {
+    r.b = length(fx);
+    ilb = r.b > R(0) ? R(1) / (L * r.b) : R(0);
+  }
   r.X0 = cross(F, fx) * ilb;
   return r;
 }
@@ -775,7 +787,12 @@ __device__ __forceinline__ void init_rk4(const DevScene& s, const RkRay<R>& ray,
   const R mb = shade_div(M, ray.b);
   const R eps = mb * mb - R(1.0 / 27.0);
   st.eps = eps;
-  st.w = copysign(sqrt(fmax(eps + g0, R(0))), ray.F1);  // g0 = x0^2 (1 + 2 x0)
+  const R P0 = fmax(eps + g0, R(0));  // w^2 at the camera; g0 = x0^2 (1 + 2 x0)
+  if constexpr (sizeof(R) == 4) {
+    st.w = copysignf(P0 > 1e-30f ? P0 * rsqrtf(P0) : 0.f, ray.F1);
+  } else {
+    st.w = copysign(sqrt(P0), ray.F1);
+  }
   st.status = kRunning;
   if (flags & kSceneDisc) {
     R A, B;
