@@ -21,6 +21,7 @@ import time
 
 PRECISIONS = {"fp32": 0, "fp64": 1, "mixed": 2}
 SCHEDULES = {"grid": 0, "persistent": 1, "hybrid": 2}
+FORMATS = {"bgra8": 0, "bgr8": 1, "rgba8": 2}
 INTEGRATORS = {"ref": 0, "rk4": 1, "flat": 2, "multi": 3}
 
 
@@ -47,11 +48,12 @@ def build_scenes(args):
     raise SystemExit(f"unknown workload {args.workload}")
 
 
-def write_ppm(path: str, bgra) -> None:
-    h, w = bgra.shape[:2]
+def write_ppm(path: str, px, rgb_first: bool = False) -> None:
+    """px: BGRA8 / BGR8 (or, rgb_first, RGBA8) frame, height x width x channels."""
+    h, w = px.shape[:2]
     with open(path, "wb") as fh:
         fh.write(f"P6\n{w} {h}\n255\n".encode())
-        fh.write(bgra[..., 2::-1].tobytes())
+        fh.write((px[..., :3] if rgb_first else px[..., 2::-1]).tobytes())
 
 
 def main(argv=None) -> int:
@@ -77,6 +79,8 @@ def main(argv=None) -> int:
                     help="MIXED + persistent or hybrid: FP32 pass, then FP64 band pass, both host-launched")
     ap.add_argument("--block", default="", help="GRID / HYBRID block shape WxH (default 8x16)")
     ap.add_argument("--rays-per-thread", type=int, default=0, help="GRID / HYBRID block tiles per block")
+    ap.add_argument("--format", default="bgra8", choices=list(FORMATS),
+                    help="frame layout (bgr8: the reference's CV_8UC3 frames)")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ppm", default="")
     args = ap.parse_args(argv)
@@ -97,13 +101,15 @@ def main(argv=None) -> int:
                                 schedule=SCHEDULES[args.schedule], step=args.step, max_steps=args.max_steps,
                                 band=args.band, setup_band=args.setup_band, slice_steps=args.slice,
                                 refill_threshold=args.refill, threads_per_block=args.threads,
-                                band_serial=int(args.band_serial), rays_per_thread=args.rays_per_thread)
+                                band_serial=int(args.band_serial), rays_per_thread=args.rays_per_thread,
+                                format=FORMATS[args.format])
     if args.block:
         opts.block_x, opts.block_y = (int(v) for v in args.block.lower().split("x"))
     with Renderer(0) as r:
         cs = r.c_scenes(scenes)
         import torch
-        bufs = [torch.empty((s.camera.height(), s.camera.width(), 4), dtype=torch.uint8, device="cuda")
+        channels = 3 if args.format == "bgr8" else 4
+        bufs = [torch.empty((s.camera.height(), s.camera.width(), channels), dtype=torch.uint8, device="cuda")
                 for s in scenes]
         frames = (capi.Frame * len(scenes))()
         for i, b in enumerate(bufs):
@@ -122,7 +128,8 @@ def main(argv=None) -> int:
         if args.ppm:
             os.makedirs(args.ppm, exist_ok=True)
             for i, b in enumerate(bufs):
-                write_ppm(os.path.join(args.ppm, f"frame_{i:04d}.ppm"), b.cpu().numpy())
+                write_ppm(os.path.join(args.ppm, f"frame_{i:04d}.ppm"), b.cpu().numpy(),
+                          rgb_first=args.format == "rgba8")
         print(json.dumps(out))
     return 0
 

@@ -29,6 +29,17 @@ def test_ppm_holds_rgb_of_bgra(tmp_path):
     assert tuple(rgb[0, 0]) == (30, 20, 10) and tuple(rgb[1, 2]) == (3, 2, 1)
 
 
+def test_ppm_of_bgr_and_rgba_frames(tmp_path):
+    bgr = np.zeros((2, 3, 3), np.uint8)
+    bgr[0, 1] = (1, 2, 3)
+    cli.write_ppm(str(tmp_path / "a.ppm"), bgr)
+    assert tuple(read_ppm(tmp_path / "a.ppm")[0, 1]) == (3, 2, 1)
+    rgba = np.zeros((2, 3, 4), np.uint8)
+    rgba[1, 2] = (7, 8, 9, 255)
+    cli.write_ppm(str(tmp_path / "b.ppm"), rgba, rgb_first=True)
+    assert tuple(read_ppm(tmp_path / "b.ppm")[1, 2]) == (7, 8, 9)
+
+
 @pytest.mark.parametrize("workload,n", [("flythrough", 3), ("objects", 2), ("flat", 2), ("binary", 2),
                                         ("single", 1), ("batched", 3)])
 def test_workloads_build(workload, n):
@@ -48,6 +59,9 @@ def test_workloads_build(workload, n):
     ["--workload", "flat", "--frames", "2", "--integrator", "flat"],
     ["--workload", "binary", "--frames", "2", "--integrator", "multi", "--step", "0.05", "--max-steps", "20000"],
     ["--workload", "binary", "--frames", "1", "--step", "0.05", "--max-steps", "20000"],  # MULTI by default
+    ["--workload", "flythrough", "--frames", "2", "--precision", "mixed", "--schedule", "hybrid", "--step", "0.15",
+     "--format", "bgr8", "--block", "32x4"],
+    ["--workload", "flythrough", "--frames", "2", "--format", "rgba8"],
 ])
 def test_cli_renders_and_writes_frames(tmp_path, capsys, renderer, argv):
     w, h = 96, 54
@@ -60,14 +74,17 @@ def test_cli_renders_and_writes_frames(tmp_path, capsys, renderer, argv):
     args = cli.argparse.Namespace(workload=argv[1], frames=frames, width=w, height=h)
     scenes = cli.build_scenes(args)
     kw = {"--integrator": ("integrator", cli.INTEGRATORS), "--precision": ("precision", cli.PRECISIONS),
-          "--schedule": ("schedule", cli.SCHEDULES)}
+          "--schedule": ("schedule", cli.SCHEDULES), "--format": ("format", cli.FORMATS)}
     opts = {"integrator": cli.INTEGRATORS[{"binary": "multi", "flat": "flat"}.get(argv[1], "rk4")]}
     for flag, (name, table) in kw.items():
         if flag in argv:
             opts[name] = table[argv[argv.index(flag) + 1]]
+    if "--block" in argv:
+        opts["block_x"], opts["block_y"] = (int(v) for v in argv[argv.index("--block") + 1].split("x"))
     for flag, name in (("--step", "step"), ("--max-steps", "max_steps")):
         if flag in argv:
             opts[name] = type(getattr(capi.default_options(), name))(argv[argv.index(flag) + 1])
     ref = renderer.render(scenes[:1], capi.default_options(**opts))[0]
     rgb = read_ppm(tmp_path / "frame_0000.ppm")
-    assert np.array_equal(rgb, ref.pixels[..., 2::-1])
+    rgba = "--format" in argv and argv[argv.index("--format") + 1] == "rgba8"
+    assert np.array_equal(rgb, ref.pixels[..., :3] if rgba else ref.pixels[..., 2::-1])

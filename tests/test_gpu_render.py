@@ -390,26 +390,29 @@ def test_host_render_in_chunks_matches_device_render(renderer):
         assert np.array_equal(px.cpu().numpy(), h.pixels)
 
 
-@pytest.mark.parametrize("schedule,fmt,rpt,band", [(capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 4, 5e-4),
-                                                   (capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 8, 0.05),
-                                                   (capi.SCHEDULE_HYBRID, capi.FORMAT_BGRA8, 4, 5e-4),
-                                                   (capi.SCHEDULE_GRID, capi.FORMAT_BGR8, 4, 5e-4),
-                                                   (capi.SCHEDULE_PERSISTENT, capi.FORMAT_BGR8, 1, 5e-4)],
-                         ids=["hybrid-bgr8", "hybrid-bgr8-r8-band0.05", "hybrid-bgra8", "grid-bgr8", "persistent-bgr8"])
-def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt, rpt, band):
+@pytest.mark.parametrize("schedule,fmt,rpt,band,precision", [
+    (capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 4, 5e-4, capi.PRECISION_MIXED),
+    (capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 8, 0.05, capi.PRECISION_MIXED),
+    (capi.SCHEDULE_HYBRID, capi.FORMAT_BGR8, 2, 5e-4, capi.PRECISION_MIXED),
+    (capi.SCHEDULE_HYBRID, capi.FORMAT_BGRA8, 4, 5e-4, capi.PRECISION_MIXED),
+    (capi.SCHEDULE_GRID, capi.FORMAT_BGR8, 4, 5e-4, capi.PRECISION_MIXED),
+    (capi.SCHEDULE_GRID, capi.FORMAT_BGR8, 4, 5e-4, capi.PRECISION_FP32),
+    (capi.SCHEDULE_PERSISTENT, capi.FORMAT_BGR8, 1, 5e-4, capi.PRECISION_MIXED)],
+    ids=["hybrid-bgr8", "hybrid-bgr8-r8-band0.05", "hybrid-bgr8-r2", "hybrid-bgra8", "grid-bgr8", "grid-fp32-bgr8",
+         "persistent-bgr8"])
+def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt, rpt, band, precision):
     """bh_render into page-locked host frames: on the GRID and HYBRID
     schedules the kernels write them directly (stats flag, no device copy;
     BGR8 rows go out as packed 32-bit words, one 32-pixel row segment per
-    warp), on the persistent schedule the frames are copied
-    back as for pageable memory; either way the frames, classes and
-    deflections equal those of the render into pageable host memory, and
-    d2h_bytes counts every byte of every buffer. Frame widths: multiples of
-    32, of 4 only (block rows partly outside the frame) and of neither
-    (rows not 4-byte aligned: pixel stores); a wide band leaves many tiles
-    with pixels the FP64 pass writes."""
+    warp), on the persistent schedule the frames are copied back as for
+    pageable memory; either way the frames, classes and deflections equal those of
+    the render into pageable host memory, and d2h_bytes counts every byte of
+    every buffer. Frame widths: multiples of 32, of 4 only (block rows partly
+    outside the frame) and of neither (rows not 4-byte aligned: pixel
+    stores); a wide band leaves many tiles with pixels the FP64 pass writes."""
     torch = pytest.importorskip("torch")
     scenes = S.flythrough(3, 320, 180) + [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1]]
-    o = opts(precision=capi.PRECISION_MIXED, schedule=schedule, format=fmt, rays_per_thread=rpt, band=band)
+    o = opts(precision=precision, schedule=schedule, format=fmt, rays_per_thread=rpt, band=band)
     ref = renderer.render(scenes, o, hit_class=True, aux=True)
     assert not renderer.stats().flags & capi.STATS_DIRECT_HOST
     bpp = 3 if fmt == capi.FORMAT_BGR8 else 4
@@ -430,6 +433,34 @@ def test_bh_render_writes_pinned_host_frames_directly(renderer, schedule, fmt, r
         assert np.array_equal(px.numpy(), r.pixels)
         assert np.array_equal(cl.numpy(), r.hit_class)
         assert np.array_equal(ax.numpy().view(np.uint32), r.aux.view(np.uint32))
+
+
+@pytest.mark.parametrize("band_serial", [0, 1, 2])
+def test_bgr8_32_wide_blocks_match_8_wide(renderer, band_serial):
+    """BGR8 frames in 32 x 4 blocks (each warp stores one 96-byte row
+    segment as packed words) against 8 x 16 blocks (packed rows of 8 pixels):
+    the same pixels and classes, for the FP32 pass launched by the band pass,
+    by the host before it (band_serial 1) and by the host after it
+    (band_serial 2); frames whose blocks cross the right or bottom edge and a
+    band wide enough to leave many warps with pixels the band pass writes."""
+    torch = pytest.importorskip("torch")
+    scenes = S.flythrough(2, 320, 180) + [S.single_scene(200, 117), S.flythrough(3, 150, 83)[1]]
+    base = dict(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_HYBRID, format=capi.FORMAT_BGR8,
+                band=0.02, step=0.15, band_serial=band_serial)
+    ref = renderer.render(scenes, opts(**base, block_x=8, block_y=16, rays_per_thread=4), hit_class=True)
+    bufs, frames = [], (capi.Frame * len(scenes))()
+    for i, s in enumerate(scenes):
+        h, w = s.camera.height(), s.camera.width()
+        px = torch.zeros((h, w, 3), dtype=torch.uint8, device="cuda")
+        cl = torch.zeros((h, w), dtype=torch.uint8, device="cuda")
+        bufs.append((px, cl))
+        frames[i] = capi.Frame(px.data_ptr(), cl.data_ptr(), None)
+    renderer.render_device(renderer.c_scenes(scenes), frames, opts(**base, block_x=32, block_y=4, rays_per_thread=8))
+    torch.cuda.synchronize()
+    assert renderer.stats().band_rays > 0
+    for (px, cl), r in zip(bufs, ref):
+        assert np.array_equal(px.cpu().numpy(), r.pixels)
+        assert np.array_equal(cl.cpu().numpy(), r.hit_class)
 
 
 def test_render_device_on_torch_stream(renderer):
