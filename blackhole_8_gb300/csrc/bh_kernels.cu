@@ -887,8 +887,9 @@ __device__ __forceinline__ bool inside(R x, const Rk4Consts<R>& c) { return x > 
 
 // Advances up to `budget` steps; returns the steps taken. kMixed (FP32 mixed
 // tracer): energy projection near the saddle and FP64 refinement of
-// crossings near the disc edges.
-template <typename R, bool kMixed>
+// crossings near the disc edges. kSliced: the persistent kernels' slices of
+// `budget` steps; a trace to the end (false) skips the budget's tests.
+template <typename R, bool kMixed, bool kSliced = true>
 __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, const Rk4Consts<R>& c,
                                            int budget) {
   constexpr bool kProject = kMixed;
@@ -904,8 +905,8 @@ __device__ __forceinline__ int advance_rk4(const DevScene& s, RayState<R>& st, c
         break;
       }
     }
-    if (taken >= budget) break;
-    const int kstop = min(min(st.kc, c.kmax), st.k + (budget - taken));
+    if (kSliced && taken >= budget) break;
+    const int kstop = kSliced ? min(min(st.kc, c.kmax), st.k + (budget - taken)) : min(st.kc, c.kmax);
     R x = st.x, w = st.w;
     int k = st.k;
     R xa = x, wa = w;
@@ -1089,7 +1090,7 @@ template <typename R, bool kMixed>
 __device__ Hit trace_rk4(const DevScene& s, int x, int y, const Rk4Consts<R>& c, int* steps) {
   RayState<R> st;
   init_rk4<R>(s, make_ray_rk4<R>(s, x, y), c.h, st);
-  *steps = advance_rk4<R, kMixed>(s, st, c, 0x7fffffff);
+  *steps = advance_rk4<R, kMixed, false>(s, st, c, 0x7fffffff);
   return finish_rk4<R>(s, st, c);
 }
 
@@ -1645,7 +1646,7 @@ __device__ __forceinline__ void grid_block(const LaunchParams& p, long long vb) 
     } else if (kPrecision == BH_PRECISION_MIXED) {
       RayState<float> st;
       if (setup_mixed(s, x, y, p, st)) {
-        steps = advance_rk4<float, true>(s, st, p.c32, 0x7fffffff);
+        steps = advance_rk4<float, true, false>(s, st, p.c32, 0x7fffffff);
         h = finish_rk4<float, true>(s, st, p.c32);
       } else if (kDefer) {
         deferred = true;
