@@ -715,7 +715,7 @@ def run_ours(args):
     fp32_steps = st_tuned.steps - st_tuned.band_steps
     # algorithmic flops of the RK4-in-phi steps (50 per step, the orbit's RK4
     # with phi advance, event compares and position recurrence) per second;
-    # the tracer itself issues 18 instructions (28 flops) per step
+    # the FP32 tracer itself issues 15 instructions (26 flops) per step
     achieved = fp32_steps * capi.RK4_ALGO_FLOPS_PER_STEP / (ms_tuned * 1e-3) / 1e12
     issue_frac = fp32_steps * capi.RK4_INSTRUCTIONS_PER_STEP / (ms_tuned * 1e-3) / (fp32_tflops * 1e12 / 2)
     variants["mixed_batched_tuned"] = {

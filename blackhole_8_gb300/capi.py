@@ -35,8 +35,8 @@ MAX_OBJECTS = 64
 MAX_HOLES = 8
 ABI_VERSION = 3
 RK4_ALGO_FLOPS_PER_STEP = 50  # BH_RK4_ALGO_FLOPS_PER_STEP: the roofline unit
-RK4_FLOPS_PER_STEP = 28
-RK4_INSTRUCTIONS_PER_STEP = 18
+RK4_FLOPS_PER_STEP = 26
+RK4_INSTRUCTIONS_PER_STEP = 15
 
 D3 = C.c_double * 3
 

