@@ -49,12 +49,12 @@ SCHEDULE_NAMES = {0: "grid", 1: "persistent", 2: "hybrid"}
 # 2e-5, 8x16 blocks, 32 rays per thread) moves per 120-frame fly-through:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size
 # (23.18 MB read, 939.96 MB written: the BGRA8 frames)
-FLYTHROUGH_DRAM_BYTES = 21.80e6 + 939.84e6
+FLYTHROUGH_DRAM_BYTES = 21.83e6 + 939.91e6
 # the same launch under ncu --set full: FP32 arithmetic instructions (FFMA +
 # FMUL + FADD lanes per cycle, 7,693) against the chip's FP32 lane-issue peak
 # (152 SMs x 128), and the FMA pipe's busy fraction
-NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.378
-NCU_FMA_PIPE_FRAC = 0.469
+NCU_FP32_INSTRUCTION_ISSUE_FRAC = 0.347
+NCU_FMA_PIPE_FRAC = 0.439
 # algorithmic bytes per ray: the 4-byte frame store and one 4-byte texel read
 ALGO_BYTES_PER_RAY = 8
 
