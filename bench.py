@@ -464,7 +464,7 @@ def adjoint_leg(r, args):
 NEAR_CRITICAL_STEPS = 20000
 
 
-def near_critical_leg(r, args, flush, threads, tuned):
+def near_critical_leg(r, args, flush, threads):
     """The near-critical stress workloads, RK4 at the oracle's step 0.01 with
     at most 20000 steps:
     - photon ring: 4096x4096, FoV 0.5 deg aimed at the photon ring; the mixed
@@ -476,7 +476,8 @@ def near_critical_leg(r, args, flush, threads, tuned):
       in FP64), with band 0 (FP32 with the FP64 first integral and the
       energy projection) and with the fly-through's tuned step, band and
       schedule, with errors on 20000 seeded rays binned by |b - b_c|.
-    The photon ring also runs with the tuned options."""
+    Each workload also runs with its own autotuned options (step, band,
+    schedule, block shape, rays per thread, band-pass block)."""
     import numpy as np
 
     from blackhole_8_gb300 import capi
@@ -498,9 +499,12 @@ def near_critical_leg(r, args, flush, threads, tuned):
     leg = {"workload": "photon ring 4096x4096, FoV 0.5 deg at r = 20 M, b within ~0.085 M of 3 sqrt(3) M, "
                        f"RK4 step 0.01, <= {NEAR_CRITICAL_STEPS} steps",
            "sample": f"every FP64-band ray ({sum(len(p) for p in band_px)}) + 4000 seeded rays"}
-    tuned_nc = capi.RenderOptions()
-    C.memmove(C.byref(tuned_nc), C.byref(tuned), C.sizeof(tuned_nc))
-    tuned_nc.max_steps = NEAR_CRITICAL_STEPS
+    def own_tuning(scene):
+        o, _ = r.autotune(r.c_scenes([scene]), capi.default_options(max_steps=NEAR_CRITICAL_STEPS),
+                          max_error=MAX_DEFLECTION_ERROR)
+        return o
+
+    tuned_nc = own_tuning(ring)
     for name, o in (("mixed", mixed), ("mixed_tuned", tuned_nc), ("plain_fp32", plain)):
         t = time_sequence(r, args, [ring], o, flush=flush)
         fb = r.render([ring], o, hit_class=True, aux=True)[0]
@@ -508,7 +512,8 @@ def near_critical_leg(r, args, flush, threads, tuned):
         err = OracleErrors()
         err.add(ring, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
         t.update({"band": o.band if o.precision == capi.PRECISION_MIXED else None, "step": o.step,
-                  "schedule": SCHEDULE_NAMES[o.schedule], "band_fraction": st.band_rays / st.rays,
+                  "schedule": SCHEDULE_NAMES[o.schedule], "threads_per_block": o.threads_per_block,
+                  "rays_per_thread": o.rays_per_thread, "band_fraction": st.band_rays / st.rays,
                   "errors_vs_cpu_oracle": err.summary(by_b=True)})
         leg[name] = t
     out["photon_ring"] = leg
@@ -518,9 +523,10 @@ def near_critical_leg(r, args, flush, threads, tuned):
     pts = np.stack([rng.integers(0, 4096, 20000), rng.integers(0, 4096, 20000)], 1)
     leg = {"workload": "impact-parameter grid 4096x4096, b uniform over 3 sqrt(3) M +- 1e-4 M, RK4 step 0.01, "
                        f"<= {NEAR_CRITICAL_STEPS} steps", "sample": "20000 seeded rays"}
+    grid_tuned = own_tuning(grid)
     for name, band in (("mixed_band_default", mixed.band), ("mixed_band_0", 0.0), ("mixed_tuned", None)):
         if band is None:
-            o = tuned_nc
+            o = grid_tuned
         else:
             o = capi.default_options(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_PERSISTENT,
                                      max_steps=NEAR_CRITICAL_STEPS, band=band)
@@ -531,6 +537,7 @@ def near_critical_leg(r, args, flush, threads, tuned):
         err = OracleErrors()
         err.add(grid, fb.hit_class, fb.aux, pts, threads, max_steps=NEAR_CRITICAL_STEPS)
         t.update({"band": o.band, "step": o.step, "schedule": SCHEDULE_NAMES[o.schedule],
+                  "threads_per_block": o.threads_per_block, "rays_per_thread": o.rays_per_thread,
                   "band_fraction": st.band_rays / st.rays, "errors_vs_cpu_oracle": err.summary(by_b=True)})
         leg[name] = t
     out["impact_grid"] = leg
@@ -786,7 +793,7 @@ def run_ours(args):
 
     near_critical = batch = None
     if not args.no_stress:
-        near_critical = near_critical_leg(r, args, flush, threads, tuned)
+        near_critical = near_critical_leg(r, args, flush, threads)
         batch = batch_leg(r, args, flush, threads, fp32_tflops)
 
     cpu = None

@@ -1385,6 +1385,16 @@ int bh_autotune(bh_ctx* ctx, const bh_scene* scenes, int32_t n, bh_render_option
       c.format = BH_FORMAT_BGRA8;
       if ((rc = time_candidate(c))) return rc;
     }
+  // the band pass's block for the fastest hybrid candidate: 512 threads (16
+  // warps per SM) suit a band of many double-float rays (impact-parameter
+  // grid 43.6 -> 40.9 ms), 256 a few long chains, which the band pass's other
+  // warps slow (photon ring 1.98 against 2.13 ms)
+  if (best_o.schedule == BH_SCHEDULE_HYBRID) {
+    bh_render_options c = best_o;
+    c.threads_per_block = 512;
+    c.format = BH_FORMAT_BGRA8;
+    if ((rc = time_candidate(c))) return rc;
+  }
   for (int rpt : {1, 4, 16}) {
     bh_render_options c = chosen;
     c.schedule = BH_SCHEDULE_GRID;

@@ -500,8 +500,12 @@ inline int render_options_problem(const bh_render_options& o, char* msg, size_t 
   if (o.band_serial < 0 || o.band_serial > 2) return bad(BH_ERR_INVALID_ARGUMENT, "band_serial must be 0, 1 or 2");
   if (o.block_x < 1 || o.block_y < 1 || o.block_x * o.block_y > 256 || (o.block_x * o.block_y) % 32 != 0)
     return bad(BH_ERR_INVALID_ARGUMENT, "grid block must hold a multiple of 32 threads, at most 256");
-  if (o.threads_per_block < 32 || o.threads_per_block > 256 || o.threads_per_block % 32 != 0)
-    return bad(BH_ERR_INVALID_ARGUMENT, "threads_per_block must be a multiple of 32 in [32, 256]");
+  // the HYBRID band pass's blocks may hold 512 threads (persistent_band_kernel's bound)
+  const int max_threads = o.schedule == BH_SCHEDULE_HYBRID ? 512 : 256;
+  if (o.threads_per_block < 32 || o.threads_per_block > max_threads || o.threads_per_block % 32 != 0)
+    return bad(BH_ERR_INVALID_ARGUMENT, o.schedule == BH_SCHEDULE_HYBRID
+                                            ? "threads_per_block must be a multiple of 32 in [32, 512] (HYBRID)"
+                                            : "threads_per_block must be a multiple of 32 in [32, 256]");
   if (o.blocks_per_sm < 0 || o.blocks_per_sm > 64) return bad(BH_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 64]");
   if (o.refill_threshold < 1 || o.refill_threshold > 32)
     return bad(BH_ERR_INVALID_ARGUMENT, "refill_threshold must be in [1, 32]");

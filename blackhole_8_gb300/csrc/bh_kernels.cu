@@ -2041,7 +2041,7 @@ __global__ void __launch_bounds__(256, 4) persistent_mixed_kernel(LaunchParams p
 // the FP32 blocks fill the rest of each SM (and the ones that do not fit
 // start as band blocks exit). The parent completes after its child, so
 // stream order holds.
-__global__ void __launch_bounds__(256) persistent_band_kernel(LaunchParams p) {
+__global__ void __launch_bounds__(512) persistent_band_kernel(LaunchParams p) {
   if (p.mixed_blocks > 0 && threadIdx.x == 0 &&
       atomicAdd(&p.counters->blocks_started, 1ull) == (unsigned long long)gridDim.x - 1ull) {
     if (p.hybrid) {

@@ -238,8 +238,8 @@ typedef struct bh_render_options {
   int32_t block_x;           /* GRID block shape (default 8 x 16: each warp an
                                 8 x 4 pixel tile) */
   int32_t block_y;
-  int32_t threads_per_block; /* PERSISTENT block size; HYBRID: the band pass's
-                                block size (default 256) */
+  int32_t threads_per_block; /* PERSISTENT block size (32..256); HYBRID: the
+                                band pass's block size (32..512, default 256) */
   int32_t blocks_per_sm;     /* PERSISTENT CTAs per SM (default: occupancy) */
   int32_t refill_threshold;  /* PERSISTENT: refill a warp once this many lanes
                                 are idle (default 32) */

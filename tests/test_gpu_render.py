@@ -463,6 +463,24 @@ def test_bgr8_32_wide_blocks_match_8_wide(renderer, band_serial):
         assert np.array_equal(cl.cpu().numpy(), r.hit_class)
 
 
+def test_hybrid_band_pass_block_sizes_agree(renderer):
+    """The HYBRID band pass in blocks of 128, 256 and 512 threads (the
+    tuner's candidates): every band ray is traced by the same code whatever
+    lane takes it, so frames, classes and deflections are identical."""
+    scenes = S.flythrough(2, 320, 180) + [S.photon_ring_scene(256)]
+    out = []
+    for threads in (128, 256, 512):
+        o = opts(precision=capi.PRECISION_MIXED, schedule=capi.SCHEDULE_HYBRID, band=0.02, step=0.175,
+                 threads_per_block=threads, rays_per_thread=8, max_steps=20000)
+        out.append(renderer.render(scenes, o, hit_class=True, aux=True))
+        assert renderer.stats().band_rays > 0
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            assert np.array_equal(a.pixels, b.pixels)
+            assert np.array_equal(a.hit_class, b.hit_class)
+            assert np.array_equal(a.aux.view(np.uint32), b.aux.view(np.uint32))
+
+
 def test_render_device_on_torch_stream(renderer):
     torch = pytest.importorskip("torch")
     scenes = [S.single_scene(64, 36)]

@@ -177,7 +177,9 @@ def test_noalloc_refuses_several_holes(lib):
 
 @pytest.mark.parametrize("bad", [{"band": float("inf")}, {"setup_band": float("inf")}, {"band": float("nan")},
                                  {"step": 0.0 - 1}, {"slice_steps": 2}, {"block_x": 7, "block_y": 1},
-                                 {"rays_per_thread": 129}, {"rays_per_thread": -1}, {"schedule": 3}])
+                                 {"rays_per_thread": 129}, {"rays_per_thread": -1}, {"schedule": 3},
+                                 {"threads_per_block": 512}, {"threads_per_block": 544, "schedule": capi.SCHEDULE_HYBRID,
+                                                              "precision": capi.PRECISION_MIXED}])
 def test_noalloc_refuses_the_options_bh_render_refuses(lib, bad):
     """The option checks are the context entry points' own: non-finite bands
     and out-of-range values are refused with the same status."""
