@@ -1551,34 +1551,21 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
   if (lane_id() == unsigned(__ffs(m) - 1) && t) atomicAdd(dst, t);
 }
 
-// BGR8 (CV_8UC3) frames. A warp whose 32 lanes hold the pixels of one block
-// of the frame -- rows of bw pixels (4, 8, 16 or 32), lane l at
-// (x0 + l % bw, y0 + l / bw) -- writes the block's 96 bytes as 24 32-bit
-// words, four pixels to three words, where byte stores would take 96 store
-// instructions per warp. `bgr` is the lane's pixel as B | G << 8 | R << 16;
-// word w of a row holds the bytes 4w .. 4w+3 of the row, which come from at
-// most two pixels. Every row must start on a 4-byte boundary (frame base
-// 4-aligned, width and x0 multiples of 4). Called by all 32 lanes.
-template <int kBw>
-__device__ __forceinline__ void store_bgr8_words_w(uint8_t* frame, int width, int x0, int y0, uint32_t bgr) {
-  constexpr int kWpr = 3 * kBw / 4;  // words per row
-  const int lane = int(lane_id());
-  const int r = lane / kWpr, w = lane - r * kWpr;  // divisions by constants
-  const int k = w % 3;
-  const int src = r * kBw + 4 * (w / 3) + k;  // the pixel of the word's first byte
-  const uint32_t a = __shfl_sync(kFull, bgr, src & 31);
-  const uint32_t b = __shfl_sync(kFull, bgr, (src + 1) & 31);
-  if (lane < 24)
-    reinterpret_cast<uint32_t*>(frame + 3 * ((long long)(y0 + r) * width + x0))[w] =
-        (a >> (8 * k)) | (b << (24 - 8 * k));
-}
-__device__ __forceinline__ void store_bgr8_words(uint8_t* frame, int width, int x0, int y0, int bw, uint32_t bgr) {
-  switch (bw) {  // the same on every lane
-    case 4: store_bgr8_words_w<4>(frame, width, x0, y0, bgr); break;
-    case 8: store_bgr8_words_w<8>(frame, width, x0, y0, bgr); break;
-    case 16: store_bgr8_words_w<16>(frame, width, x0, y0, bgr); break;
-    default: store_bgr8_words_w<32>(frame, width, x0, y0, bgr); break;
-  }
+// BGR8 (CV_8UC3) frames. In a warp whose lanes hold rows of pixels in
+// order (rows of 4, 8, 16 or 32 pixels starting at a multiple of 4 in x:
+// lane l + 1 holds the right neighbour of lane l unless x % 4 == 3), the
+// lanes with k = x % 4 < 3 write the 32-bit word that starts k bytes into
+// their own pixel (byte 3 x + k; four pixels make three words): bytes k .. 2
+// of their pixel and the first k + 1 of the next lane's, one shuffle and 24
+// word stores per 32 pixels where byte stores would take 96. `bgr` is the
+// lane's pixel as B | G << 8 | R << 16. Rows must start on 4-byte
+// boundaries (frame base 4-aligned, width a multiple of 4). Called by all 32
+// lanes.
+__device__ __forceinline__ void store_bgr8_words(uint8_t* frame, int width, int x, int y, uint32_t bgr) {
+  const uint32_t next = __shfl_down_sync(kFull, bgr, 1);
+  const int k = x & 3;
+  if (k < 3)
+    *reinterpret_cast<uint32_t*>(frame + 3 * ((long long)y * width + x) + k) = (bgr >> (8 * k)) | (next << (24 - 8 * k));
 }
 
 __device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
@@ -1588,8 +1575,9 @@ __device__ __forceinline__ uint32_t bgr_word(const Hit& h) {
 // True when store_bgr8_words can write the warp's pixels: the GRID kernels'
 // warps cover whole rows of bw pixels (lane l at (x0 + l % bw, y0 + l / bw),
 // x0 a multiple of bw, so of 4), and then it takes every lane's pixel in the
-// frame (`valid`) and frame rows that start on 4-byte boundaries. Called by
-// all 32 lanes; the result is the same on every lane.
+// frame (`valid`: the next lane's pixel is part of the word) and frame rows
+// that start on 4-byte boundaries. Called by all 32 lanes; the result is the
+// same on every lane.
 __device__ __forceinline__ bool bgr8_block_ok(const DevScene& s, bool valid) {
   return __all_sync(kFull, valid) && (s.hot_i.y & 3) == 0 && (reinterpret_cast<uintptr_t>(s.pixels) & 3) == 0;
 }
@@ -1623,10 +1611,10 @@ __device__ __forceinline__ void grid_store(const DevScene& s, int format, int x,
   if (format == BH_FORMAT_BGR8) {
     // warps cover whole rows of bw pixels: block rows of a multiple of 32
     // pixels, or of 4, 8 or 16 (powers of two dividing 32)
-    const int bx = int(blockDim.x), bw = bx < 32 ? bx : 32;
+    const int bx = int(blockDim.x);
     const bool rows = (bx & 31) == 0 || (bx >= 4 && bx < 32 && (bx & (bx - 1)) == 0);
     if (rows && bgr8_block_ok(s, valid)) {
-      store_bgr8_words(s.pixels, s.hot_i.y, __shfl_sync(kFull, x, 0), __shfl_sync(kFull, y, 0), bw, bgr_word(h));
+      store_bgr8_words(s.pixels, s.hot_i.y, x, y, bgr_word(h));
       store_extras(s, x, y, h);
       return;
     }
