@@ -5,8 +5,9 @@
 // plane through the hole (:170-193; the basis is orthonormal, so the
 // reference's 3x3 inverse is a transpose here), (3) integrates the photon
 // orbit with either the reference's 20+20-step trapezoid rule in u with chord
-// collisions (:202-296) or classical RK4 in phi on u'' = -u + 3 u^2 (u = M/r)
-// with horizon, escape and disc-plane events, (4) samples the disc or
+// collisions (:202-296) or fixed fourth-order steps in phi on
+// u'' = -u + 3 u^2 (u = M/r; classical RK4 in FP64, Nystrom's three-stage
+// method in FP32) with horizon, escape and disc-plane events, (4) samples the disc or
 // background texture and (5) stores the pixel.
 //
 // RK4 details. The state is x = u - 1/3, w = du/dphi: the orbit equation
