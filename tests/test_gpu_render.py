@@ -463,6 +463,28 @@ def test_bgr8_32_wide_blocks_match_8_wide(renderer, band_serial):
         assert np.array_equal(cl.cpu().numpy(), r.hit_class)
 
 
+def test_fp32_step_is_fourth_order(renderer):
+    """The FP32 tracers' step (Nystrom's three-stage method) is fourth order:
+    against FP64 RK4 at step 0.01, halving the step from 0.2 to 0.1 divides
+    the largest deflection error of the escaped rays away from b_c
+    (|b - b_c| > 0.5 M, where FP32 rounding stays far below the truncation)
+    by about 2^4 = 16; at least 6 here, and at step 0.2 that error is below
+    the 1e-4 rad bound."""
+    sc = S.flythrough(3, 320, 180)[1]
+    h, w = sc.camera.height(), sc.camera.width()
+    ys, xs = np.mgrid[0:h, 0:w]
+    far = (np.abs(S.ref_impact_parameter(sc, xs.ravel(), ys.ravel()) - 3.0 * 3.0 ** 0.5) > 0.5).reshape(h, w)
+    ref = renderer.render([sc], opts(precision=capi.PRECISION_FP64, step=0.01), hit_class=True, aux=True)[0]
+    errs = []
+    for step in (0.2, 0.1):
+        out = renderer.render([sc], opts(precision=capi.PRECISION_FP32, step=step), hit_class=True, aux=True)[0]
+        m = far & (out.hit_class == capi.CLASS_MISS) & (ref.hit_class == capi.CLASS_MISS)
+        assert m.sum() > 1000
+        errs.append(float(np.abs(out.aux[m].astype(np.float64) - ref.aux[m]).max()))
+    assert errs[0] < 1e-4
+    assert errs[0] / errs[1] > 6.0, errs
+
+
 def test_hybrid_band_pass_block_sizes_agree(renderer):
     """The HYBRID band pass in blocks of 128, 256 and 512 threads (the
     tuner's candidates): every band ray is traced by the same code whatever
