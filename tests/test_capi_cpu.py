@@ -56,6 +56,7 @@ int main(void) {
          offsetof(bh_render_options, band_serial));
   printf("%zu %zu %zu %d %d\n", offsetof(bh_scene, objects), offsetof(bh_scene, n_extra_holes),
          offsetof(bh_scene, extra_holes), BH_MAX_HOLES, BH_INTEGRATOR_MULTI);
+  printf("%d %d %d\n", BH_RK4_ALGO_FLOPS_PER_STEP, BH_RK4_FLOPS_PER_STEP, BH_RK4_INSTRUCTIONS_PER_STEP);
   return 0;
 }
 ''')
@@ -72,6 +73,9 @@ int main(void) {
                     capi.RenderOptions.band_serial.offset]
     assert list(map(int, out[2].split())) == [capi.Scene.objects.offset, capi.Scene.n_extra_holes.offset,
                                               capi.Scene.extra_holes.offset, capi.MAX_HOLES, capi.INTEGRATOR_MULTI]
+    # the roofline's per-step constants the bench reports
+    assert list(map(int, out[3].split())) == [capi.RK4_ALGO_FLOPS_PER_STEP, capi.RK4_FLOPS_PER_STEP,
+                                              capi.RK4_INSTRUCTIONS_PER_STEP]
 
 
 def test_create_without_device_reports_no_device(lib):
