@@ -824,6 +824,10 @@ int render_direct_to_host(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const 
   if (od.format == BH_FORMAT_BGR8 && od.block_x < 32) {
     od.block_y = std::max(1, od.block_x * od.block_y / 32);
     od.block_x = 32;
+    // and at most 32 tiles per thread: on the 120-frame 1080p fly-through
+    // into pinned frames 4 / 8 / 16 / 32 / 64 / 128 took 6.1 / 5.7 / 5.55 /
+    // 5.57 / 5.67 / 5.79 ms, where the device-frame optimum is 32-64
+    od.rays_per_thread = std::min(od.rays_per_thread, 32);
   }
   int rc = render_on_device(ctx, scenes, n, hf.data(), od, ctx->stream, true);
   if (rc) return rc;

@@ -318,8 +318,9 @@ int bh_texture_destroy(bh_ctx* ctx, int32_t id);
  * cudaMallocHost or cudaHostRegister) and the schedule is GRID or HYBRID,
  * the kernels write the frames there directly (no device copy, no
  * copy-back; stats flag BH_STATS_DIRECT_HOST); BGR8 frames are then written
- * with blocks 32 pixels wide (same threads per block), so that each warp
- * stores whole 96-byte row segments over the host link.
+ * with blocks 32 pixels wide (same threads per block) and at most 32 tiles
+ * per thread, so that each warp stores whole 96-byte row segments over the
+ * host link.
  * bh_render_device: frames in device memory; enqueued on `stream` (a
  * cudaStream_t, NULL = the context's stream) and returns without waiting. */
 int bh_render(bh_ctx* ctx, const bh_scene* scenes, int32_t n, const bh_frame* frames,
